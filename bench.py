@@ -1,0 +1,298 @@
+"""Benchmark: bond additions per second of the Newman-Ziff ensemble at L=256.
+
+One step = one batch of R independent runs on spanning_2d_grid(256)
+(N = 65,536 sites, M = 130,560 bonds) through the whole hot path: Philox
+permutations, union-find with per-step statistics, fused microcanonical
+run-reductions, banded canonical convolution at 1001 uniform p in [0, 1],
+and the pairwise merge into the running (n, mean, M2) averages.
+value = R * M * n_gpus / step time (bond additions per second).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference pipeline
+(oracle/, threaded over all host cores) on the same lattice and p-grid.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+L_DEFAULT = 256
+P_DEFAULT = 1001
+KEY = 1234
+# algorithmic DRAM bytes per bond addition of the union-find kernel: four
+# random 32-byte sectors (find(u), find(v), the child pointer and the root
+# word written on a union) plus the 36 bytes of per-step records it streams
+UF_BYTES_PER_ADD = 4 * 32 + 36
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--runs', type=int, default=100000, help='runs per step per GPU')
+    ap.add_argument('--L', type=int, default=L_DEFAULT)
+    ap.add_argument('--P', type=int, default=P_DEFAULT)
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
+    ap.add_argument('--no-micro', action='store_true')
+    ap.add_argument('--window', type=int, default=0)
+    ap.add_argument('--cpu-sample', type=int, default=256, help='runs in the CPU baseline sample')
+    ap.add_argument('--e2e-steps', type=int, default=2)
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d['hbm_gbs']), 'measured'
+    return 6800.0, 'fallback'
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith('active'):
+                    reasons.add(name)
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': float(max(smax)) if smax else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def cpu_baseline(L, ps, sample, threads=None):
+    """The oracle's threaded CPU pipeline on a bounded sample of runs."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    N, M = O.lattice_size(O.GRID_2D, L)
+    bands = O.band_table(M, ps)
+    t0 = time.perf_counter()
+    O.ensemble_canonical(O.GRID_2D, L, KEY, 10 ** 9, sample, ps, n_threads=threads, bands=bands)
+    dt = time.perf_counter() - t0
+    return {'value': sample * M / dt, 'unit': 'bond additions/s', 'cores': threads,
+            'kind': 'port',
+            'sample': '%d runs of spanning_2d_grid(%d), %d p, union-find + FP64 banded '
+                      'canonical convolution + pairwise merge (oracle/nz_oracle.c)' %
+                      (sample, L, len(ps))}
+
+
+def dist_setup(args):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    L = args.L
+    ps = np.linspace(0.0, 1.0, args.P)
+    N, M = O.lattice_size(O.GRID_2D, L)
+    threads = os.cpu_count() or 1
+    bands = O.band_table(M, ps)
+    sample = max(threads * 4, 16)
+    for _ in range(args.warmup):
+        O.ensemble_canonical(O.GRID_2D, L, KEY, 0, threads, ps, n_threads=threads, bands=bands)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        O.ensemble_canonical(O.GRID_2D, L, KEY, k * sample, sample, ps, n_threads=threads,
+                             bands=bands)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = sample * M / dt
+    line = {
+        'impl': 'reference', 'metric': 'bond additions/s', 'value': value,
+        'unit': 'bond additions/s', 'n_gpus': args.gpus, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': dt * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'int64/u128 + f64',
+        'data': 'synthetic (Philox permutations)',
+        'config': {'workload': 'spanning_2d_grid(%d), %d uniform p, bounded sample of %d runs '
+                               'per step on the host cores' % (L, args.P, sample),
+                   'L': L, 'P': args.P, 'runs_per_step': sample},
+        'cpu_baseline': {'value': value, 'unit': 'bond additions/s', 'cores': threads,
+                         'kind': 'port',
+                         'sample': '%d runs per step (oracle/nz_oracle.c restatement of '
+                                   'percolate/hpc.py, pthreads over all cores)' % sample},
+        'e2e': {'value': value, 'unit': 'bond additions/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    from pypercolate_gb300 import _native as nat
+    from pypercolate_gb300.ensemble import Ensemble
+
+    L, R = args.L, args.runs
+    ps = np.linspace(0.0, 1.0, args.P)
+    N, M = L * L, 2 * L * (L - 1)
+    ens = Ensemble('grid', L, ps, precision=args.precision, micro=not args.no_micro,
+                   window=args.window)
+    run_base = rank * 10 ** 9  # disjoint run ids per rank (weak scaling)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for w in range(args.warmup):
+        ens.run(R, key=KEY, run0=run_base + w * R)
+    torch.cuda.synchronize()
+    nat.profile_read()
+    nat.profile_enable(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        ens.run(R, key=KEY, run0=run_base + (args.warmup + k) * R)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    nat.profile_enable(False)
+    prof = nat.profile_read()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device='cuda')
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = R * M * world / (ms * 1e-3)
+
+    # dominant kernel: union-find windows
+    uf_n, uf_ms = prof['union_find']
+    adds_per_launch = R * M / max(uf_n / args.steps, 1)
+    uf_avg_s = uf_ms / max(uf_n, 1) * 1e-3
+    achieved = UF_BYTES_PER_ADD * adds_per_launch / uf_avg_s / 1e9
+    peak, peak_kind = peaks()
+    launches = {k: v[0] for k, v in prof.items()}
+    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 1, 'reduce': 4}
+    gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
+
+    # end to end through the public API: inputs (p-grid) from pinned host
+    # memory, results (finalized canonical averages) read back every step
+    h_ps = torch.from_numpy(ps.copy()).pin_memory()
+    h2d = h_ps.numel() * 8
+    d2h = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        e = Ensemble('grid', L, h_ps.numpy(), precision=args.precision,
+                     micro=not args.no_micro, window=args.window)
+        e._ws = ens._ws  # reuse the device workspace
+        e.d_ps.copy_(h_ps, non_blocking=True)
+        e.run(R, key=KEY, run0=run_base + 10 ** 8 + k * R)
+        fin = e.finalized(0.05)
+        d2h = fin.nbytes + e.canonical_averages().nbytes
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_value = R * M * world / e2e_s
+
+    line = {
+        'metric': 'bond additions/s', 'value': value, 'unit': 'bond additions/s',
+        'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'int32 union-find, u64/u128 moments, %s convolution' % args.precision,
+        'data': 'synthetic (Philox-4x32-10 keyed permutations, seed %d)' % KEY,
+        'config': {'workload': 'spanning_2d_grid(%d) batched ensemble: %d runs/step/GPU, '
+                               '%d uniform p in [0,1], fused micro reductions=%s'
+                               % (L, R, args.P, not args.no_micro),
+                   'L': L, 'N': N, 'M': M, 'runs_per_step': R, 'P': args.P,
+                   'precision': args.precision,
+                   'l2': 'inputs larger than L2 (%.1f GB of union-find state per step)'
+                         % (R * N * 4 / 1e9)},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': None,
+                     'kernel': 'uf_window_kernel', 'peak_source': peak_kind,
+                     'bytes_per_addition': UF_BYTES_PER_ADD,
+                     'avg_launch_ms': uf_avg_s * 1e3},
+        'kernel_ms_per_step': {k: v[1] / args.steps for k, v in prof.items()},
+        'clocks': clocks,
+        'gpu_launches': gpu_launches,
+        'e2e': {'value': e2e_value, 'unit': 'bond additions/s', 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h},
+    }
+    if rank == 0:
+        try:
+            line['cpu_baseline'] = cpu_baseline(L, ps, args.cpu_sample)
+        except Exception as exc:  # the oracle is a measurement aid only
+            line['cpu_baseline'] = {'value': None, 'error': repr(exc)}
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

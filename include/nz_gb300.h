@@ -1,0 +1,237 @@
+/*
+ * nz_gb300.h -- C ABI of the GB300 Newman-Ziff bond-percolation library
+ * (libnzgb300.so, sources in pypercolate_gb300/csrc/).
+ *
+ * The library replaces the `percolate.hpc` path of andsor/pypercolate 0.4.6.
+ * Every entry point:
+ *   - takes plain pointers and sizes (device pointers unless a name says
+ *     "host"), never throws, and returns an NZ_* status code;
+ *   - is stream-ordered on the `stream` argument (a cudaStream_t, NULL = the
+ *     legacy default stream) and does not synchronise unless stated;
+ *   - allocates nothing: the caller owns every buffer, including scratch,
+ *     whose size the *_workspace_bytes functions report.
+ * Calls on one stream are serialised by the stream; concurrent calls on
+ * different streams must not share output or workspace buffers.
+ *
+ * Statistic order used by all canonical entry points (7 per p):
+ *   0 percolation_probability (spanning), 1 max_cluster_size,
+ *   2..6 moments k = 0..4 (largest cluster excluded).
+ */
+#ifndef NZ_GB300_H
+#define NZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------- */
+#define NZ_OK 0
+#define NZ_ERR_INVALID 1        /* invalid argument (Python: ValueError)       */
+#define NZ_ERR_SPANNING_SIDES 2 /* spanning requested, graph lacks two sides
+                                   (percolate/hpc.py:197-202: ValueError)     */
+#define NZ_ERR_TOO_LARGE 3      /* beyond a documented size limit              */
+#define NZ_ERR_CUDA 4           /* a CUDA runtime call failed                  */
+#define NZ_ERR_WORKSPACE 5      /* workspace smaller than required             */
+
+/* ---- graph kinds ---------------------------------------------------- */
+#define NZ_GRAPH_GRID2D 0  /* spanning_2d_grid(L), percolate/percolate.py:931-965 */
+#define NZ_GRAPH_CHAIN1D 1 /* spanning_1d_chain(l), percolate/percolate.py:899-928 */
+#define NZ_GRAPH_EDGES 2   /* explicit edge list (any perc_graph)              */
+
+/* ---- permutation sources -------------------------------------------- */
+#define NZ_PERM_PHILOX 0  /* Philox-4x32-10-keyed Feistel bijection: run r uses
+                             key `key`, counter run_id = run0 + r             */
+#define NZ_PERM_GIVEN 1   /* caller-supplied perms[r * M + n]                 */
+#define NZ_PERM_MT19937 2 /* np.random.RandomState(seed).permutation(M),
+                             percolate/hpc.py:195,206                         */
+
+/* Size limits (checked; NZ_ERR_TOO_LARGE beyond them). */
+#define NZ_MAX_NODES (1u << 21)   /* node ids and exact u64 sums of s^3 */
+#define NZ_MAX_RUNS (1u << 24)
+
+/* Graph descriptor.  For NZ_GRAPH_GRID2D / NZ_GRAPH_CHAIN1D only `kind` and
+ * `length` are read (N and M are derived); the edge numbering equals the
+ * order of networkx's perc_graph.edges() for the reference's builders. */
+typedef struct NzGraph {
+    int32_t kind;
+    uint32_t length;          /* L (grid) or l (chain)                        */
+    uint32_t num_nodes;       /* N, NZ_GRAPH_EDGES only                       */
+    uint32_t num_edges;       /* M, NZ_GRAPH_EDGES only                       */
+    const uint32_t *edge_u;   /* device [M], NZ_GRAPH_EDGES only              */
+    const uint32_t *edge_v;   /* device [M]                                   */
+    const uint8_t *node_side; /* device [N]: bit 0 touches side 0, bit 1 side 1 */
+} NzGraph;
+
+/* Per-step records of one window of steps for a batch of runs.  Each plane
+ * is n-major with the run index fastest: element (n, r) is at
+ * plane[(n - n_base) * run_stride + r].  Any plane may be NULL. */
+typedef struct NzRecords {
+    uint32_t *max_span; /* bits 0..30 max cluster size, bit 31 has_spanning   */
+    uint32_t *m0;       /* number of clusters - 1                             */
+    uint64_t *m2;       /* sum' s^2  (sum over clusters, largest excluded)    */
+    uint64_t *m3;       /* sum' s^3                                           */
+    uint64_t *m4_lo;    /* sum' s^4, low 64 bits (the reference's uint64)     */
+    uint32_t *m4_hi;    /* sum' s^4, bits 64..95                              */
+    uint32_t *edge;     /* edge index added at step n (0 at n = 0)            */
+    int64_t run_stride;
+} NzRecords;
+
+/* ---- library -------------------------------------------------------- */
+const char *nz_version(void);
+const char *nz_status_string(int status);
+/* Fills N and M for a descriptor (host call, no device work). */
+int nz_graph_size(const NzGraph *graph, uint32_t *num_nodes, uint32_t *num_edges);
+
+/* ---- microcanonical statistics -------------------------------------- */
+/* Replaces percolate/hpc.py:310-404 bond_microcanonical_statistics (and the
+ * generator percolate/hpc.py:73-307 bond_sample_states, whose rows are the
+ * same) for n_runs independent runs at once.  Writes rows n = 0..M.
+ *   spanning      : detect a spanning cluster (needs two sides).
+ *   perm_mode     : NZ_PERM_*.
+ *   key, run0     : Philox key and first run id (NZ_PERM_PHILOX).
+ *   perms         : device [n_runs * M] (NZ_PERM_GIVEN).
+ *   mt_seed_words : device [n_runs * mt_words_stride] seed words and
+ *   mt_seed_len   : device [n_runs]; len 0 = scalar seed word[0]
+ *                   (init_genrand), len k >= 1 = array seed (init_by_array).
+ *   workspace     : device scratch of nz_microcanonical_workspace_bytes().
+ */
+size_t nz_microcanonical_workspace_bytes(const NzGraph *graph, int32_t n_runs,
+                                         int32_t perm_mode);
+int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs,
+                      int32_t perm_mode, uint64_t key, uint64_t run0,
+                      const uint32_t *perms, const uint32_t *mt_seed_words,
+                      const int32_t *mt_seed_len, int32_t mt_words_stride,
+                      void *workspace, size_t workspace_bytes,
+                      const NzRecords *out, void *stream);
+
+/* Writes the permutations the runs would use (for checking and for
+ * NZ_PERM_GIVEN replays): out[r * M + n]. */
+int nz_permutations(uint32_t num_edges, int32_t n_runs, int32_t perm_mode,
+                    uint64_t key, uint64_t run0, const uint32_t *mt_seed_words,
+                    const int32_t *mt_seed_len, int32_t mt_words_stride,
+                    uint32_t *out, void *stream);
+
+/* Packs run `run` of a record set into the reference's structured rows
+ * (percolate/hpc.py:34-70 microcanonical_statistics_dtype, packed, 53 bytes
+ * with the spanning field, 52 without): rows[n * row_bytes ...]. */
+int nz_pack_microcanonical_rows(const NzRecords *rec, int32_t run,
+                                uint32_t num_nodes, uint32_t num_edges,
+                                int32_t spanning, uint8_t *rows, void *stream);
+
+/* ---- canonical statistics ------------------------------------------- */
+/* Banded normalised binomial weights B(M, n, p) (percolate/percolate.py:
+ * 1067-1109 _binomial_pmf) in FP64 from log-binomials, for P values of p.
+ * Band of p_i: n in [band_lo[i], band_lo[i] + band_len[i]), the n where
+ * log B >= log B(mode) - cutoff; weights[i * cap + j] for j < band_len[i]
+ * (zero-filled to cap).  Returns NZ_ERR_TOO_LARGE if a band exceeds cap.
+ * nz_binomial_band_cap() is a safe cap for (M, cutoff). */
+int32_t nz_binomial_band_cap(uint32_t num_edges, double cutoff);
+int nz_binomial_weights(uint32_t num_edges, const double *ps, int32_t P,
+                        double cutoff, int32_t cap, uint32_t *band_lo,
+                        uint32_t *band_len, double *weights, void *stream);
+
+/* Full-length FP64 pmf vectors: out[i * (M + 1) + n] (the reference's own
+ * convolution_factors layout). */
+int nz_binomial_pmf(uint32_t num_edges, const double *ps, int32_t P,
+                    double *out, void *stream);
+
+/* Replaces percolate/hpc.py:443-515 bond_canonical_statistics on rows in the
+ * reference's packed layout: out[i * 7 + s] = sum_n f_i[n] * Q_s[n] for
+ * n_factor_sets full-length factor vectors (factors[i * (M + 1) + n]), FP64. */
+int nz_canonical_statistics_rows(const uint8_t *rows, uint32_t num_edges,
+                                 int32_t spanning, const double *factors,
+                                 int32_t n_factor_sets, double *out,
+                                 void *stream);
+
+/* Canonical statistics of records (runs r < n_runs, all n = 0..M), FP64,
+ * banded weights: out[(r * P + i) * 7 + s]. */
+int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes,
+                                    uint32_t num_edges, int32_t n_runs,
+                                    int32_t spanning, const uint32_t *band_lo,
+                                    const uint32_t *band_len,
+                                    const double *weights, int32_t cap,
+                                    int32_t P, double *out, void *stream);
+
+/* ---- averages (n, mean, M2) ------------------------------------------ */
+/* Canonical-averages rows use the layout of percolate/hpc.py:518-558
+ * (number_of_runs u32, then per statistic mean f8, m2 f8; packed).
+ * These entry points work on that byte layout directly. */
+
+/* percolate/hpc.py:561-635 bond_initialize_canonical_averages: packed
+ * canonical_statistics rows (hpc.py:407-440) -> canonical_averages rows. */
+int nz_initialize_canonical_averages(const uint8_t *canonical_rows, int32_t P,
+                                     int32_t spanning, uint8_t *out_rows,
+                                     void *stream);
+/* percolate/hpc.py:638-702 bond_reduce: pairwise merge of two row sets. */
+int nz_bond_reduce(const uint8_t *rows_a, const uint8_t *rows_b, int32_t P,
+                   int32_t spanning, uint8_t *out_rows, void *stream);
+/* percolate/hpc.py:752-834 finalize_canonical_averages: mean (/N),
+ * std = sqrt(M2/(n-1)) (/N), Student-t interval at 1 - alpha; NaN where the
+ * reference's scipy call yields NaN. */
+int nz_finalize_canonical_averages(const uint8_t *avg_rows, int32_t P,
+                                   int32_t spanning, double number_of_nodes,
+                                   const double *ps, double alpha,
+                                   uint8_t *out_rows, void *stream);
+
+/* Student-t quantile t_{q}(df) for each element (device math, FP64). */
+int nz_student_t_quantile(const double *q, const double *df, int32_t count,
+                          double *out, void *stream);
+
+/* ---- ensemble (batched fast path) ------------------------------------ */
+/* Microcanonical run-reduction accumulators for one lattice size, per
+ * n = 0..M (percolate/percolate.py:450-705 semantics): exact integer sums
+ * and FP64 sums of squared deviations (pairwise-merged). */
+typedef struct NzMicroAccum {
+    uint64_t *count;     /* [1] runs accumulated                            */
+    uint64_t *span_count;/* [M+1] runs with a spanning cluster               */
+    uint64_t *sum_lo;    /* [6][M+1] exact sums of max, m0..m4, low words    */
+    uint64_t *sum_hi;    /* [6][M+1] high words                              */
+    double *m2;          /* [6][M+1] sums of squared deviations from the mean */
+} NzMicroAccum;
+
+/* Microcanonical averages (percolate/percolate.py:450-705 and 968-1064
+ * microcanonical_averages / microcanonical_averages_arrays) from the
+ * accumulators: out[n * 21 + j], n = 0..M, j = spanning (mean, lo, hi) --
+ * Bayesian (k+1)/(R+2) with Beta quantiles --, then max, m0..m4 (mean, lo,
+ * hi) divided by num_nodes, Student-t intervals ((mean, mean) if std == 0). */
+int nz_microcanonical_finalize(const NzMicroAccum *acc, uint32_t num_nodes,
+                               uint32_t num_edges, int32_t spanning,
+                               double alpha, double *out, void *stream);
+
+/* The whole per-lattice pipeline for n_runs Philox runs:
+ * permutation -> union-find -> (optional) fused microcanonical reductions
+ * -> banded canonical convolution at P probabilities -> pairwise merge.
+ * Results are merged into (acc_count, acc_mean[P*7], acc_m2[P*7]) and, if
+ * micro != NULL, into *micro.  conv_precision: 0 = FP64, 1 = FP32 with
+ * FP64 chunk accumulation. */
+size_t nz_ensemble_workspace_bytes(const NzGraph *graph, int32_t n_runs,
+                                   int32_t P, int32_t window);
+int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
+                uint64_t key, uint64_t run0, const double *ps, int32_t P,
+                double cutoff, int32_t window, int32_t conv_precision,
+                void *workspace, size_t workspace_bytes, uint64_t *acc_count,
+                double *acc_mean, double *acc_m2, const NzMicroAccum *micro,
+                void *stream);
+
+/* ---- measurement ------------------------------------------------------ */
+/* When enabled, every launch sequence of a category below is bracketed by
+ * CUDA events recorded on the caller's stream.  nz_profile_read waits for
+ * the recorded events, returns per category the number of bracketed
+ * sequences and their summed elapsed milliseconds, and clears the record.
+ * (The project's own instrumentation; no counterpart in the reference.) */
+#define NZ_PROF_SETUP 0      /* weights, run initialisation                 */
+#define NZ_PROF_UNION_FIND 1 /* uf_window_kernel                            */
+#define NZ_PROF_MICRO 2      /* fused microcanonical reductions             */
+#define NZ_PROF_CONV 3       /* banded canonical convolution                */
+#define NZ_PROF_REDUCE 4     /* merge over runs                             */
+#define NZ_PROF_CATEGORIES 5
+void nz_profile_enable(int32_t enabled);
+int nz_profile_read(int32_t n_categories, int64_t *launches, double *total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NZ_GB300_H */

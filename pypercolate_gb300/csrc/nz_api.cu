@@ -1,0 +1,457 @@
+// nz_api.cu -- the extern "C" entry points of libnzgb300.so (include/nz_gb300.h).
+//
+// Host-side orchestration: argument validation, workspace carving, launch
+// sequencing on the caller's stream.  Nothing here allocates device memory.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "nz_common.cuh"
+#include "nz_internal.cuh"
+
+using namespace nz;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+
+inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+struct Carver {
+    uint8_t *base;
+    size_t used;
+    size_t cap;
+    template <class T>
+    T *take(size_t count) {
+        size_t off = align_up(used);
+        used = off + count * sizeof(T);
+        return base ? reinterpret_cast<T *>(base + off) : nullptr;
+    }
+    bool ok() const { return used <= cap; }
+};
+
+inline int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NZ_OK : NZ_ERR_CUDA;
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- optional per-kernel timing (CUDA events on the launching stream) ----
+struct ProfState {
+    std::mutex mu;
+    bool enabled = false;
+    std::vector<cudaEvent_t> pool;
+    struct Rec { int cat; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    cudaEvent_t get() {
+        if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+};
+ProfState g_prof;
+
+struct ProfScope {
+    int cat;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(int c, cudaStream_t st) : cat(c), s(st) {
+        if (!g_prof.enabled) return;
+        std::lock_guard<std::mutex> lk(g_prof.mu);
+        a = g_prof.get();
+        b = g_prof.get();
+        cudaEventRecord(a, s);
+    }
+    ~ProfScope() {
+        if (!a) return;
+        cudaEventRecord(b, s);
+        std::lock_guard<std::mutex> lk(g_prof.mu);
+        g_prof.recs.push_back({cat, a, b});
+    }
+};
+
+constexpr uint32_t kRecordBytes = 4 + 4 + 8 + 8 + 8 + 4;  // planes without edge
+
+// Workspace of the microcanonical entry point.
+size_t micro_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t perm_mode, uint32_t **nodes,
+                    RunState **state, uint32_t **flag, uint32_t **perms) {
+    *nodes = c.take<uint32_t>((size_t)n_runs * g.N);
+    *state = c.take<RunState>((size_t)n_runs);
+    *flag = c.take<uint32_t>(4);
+    *perms = perm_mode == NZ_PERM_MT19937 ? c.take<uint32_t>((size_t)n_runs * (g.M ? g.M : 1)) : nullptr;
+    return c.used;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *nz_version(void) { return "pypercolate-gb300 0.1.0 (sm_103a)"; }
+
+const char *nz_status_string(int status) {
+    switch (status) {
+        case NZ_OK: return "ok";
+        case NZ_ERR_INVALID: return "invalid argument";
+        case NZ_ERR_SPANNING_SIDES:
+            return "Spanning cluster is to be detected, but auxiliary nodes of less or more than 2 types (sides) given.";
+        case NZ_ERR_TOO_LARGE: return "size beyond the library's limits";
+        case NZ_ERR_CUDA: return "CUDA runtime error";
+        case NZ_ERR_WORKSPACE: return "workspace too small";
+        default: return "unknown status";
+    }
+}
+
+int nz_graph_size(const NzGraph *graph, uint32_t *num_nodes, uint32_t *num_edges) {
+    if (!graph || !num_nodes || !num_edges) return NZ_ERR_INVALID;
+    return graph_size(*graph, *num_nodes, *num_edges);
+}
+
+size_t nz_microcanonical_workspace_bytes(const NzGraph *graph, int32_t n_runs, int32_t perm_mode) {
+    uint32_t N, M;
+    if (!graph || graph_size(*graph, N, M) != NZ_OK || n_runs <= 0) return 0;
+    GraphDev g = make_graph_dev(*graph, N, M);
+    Carver c{nullptr, 0, 0};
+    uint32_t *a, *f, *p;
+    RunState *st;
+    return align_up(micro_layout(c, g, n_runs, perm_mode, &a, &st, &f, &p));
+}
+
+int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs, int32_t perm_mode, uint64_t key,
+                      uint64_t run0, const uint32_t *perms, const uint32_t *mt_seed_words,
+                      const int32_t *mt_seed_len, int32_t mt_words_stride, void *workspace,
+                      size_t workspace_bytes, const NzRecords *out, void *stream) {
+    if (!graph || !out || n_runs <= 0) return NZ_ERR_INVALID;
+    if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
+    uint32_t N, M;
+    int st = graph_size(*graph, N, M);
+    if (st) return st;
+    if (perm_mode == NZ_PERM_GIVEN && M > 0 && !perms) return NZ_ERR_INVALID;
+    if (perm_mode == NZ_PERM_MT19937 && (!mt_seed_words || !mt_seed_len)) return NZ_ERR_INVALID;
+    if (perm_mode < 0 || perm_mode > 2) return NZ_ERR_INVALID;
+    if (!out->max_span || !out->m0 || !out->m2 || !out->m3 || !out->m4_lo || out->run_stride < n_runs)
+        return NZ_ERR_INVALID;
+    GraphDev g = make_graph_dev(*graph, N, M);
+    Carver c{static_cast<uint8_t *>(workspace), 0, workspace_bytes};
+    uint32_t *nodes, *flag, *mt_perms;
+    RunState *state;
+    micro_layout(c, g, n_runs, perm_mode, &nodes, &state, &flag, &mt_perms);
+    if (!workspace || !c.ok()) return NZ_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+    launch_init_runs(g, n_runs, nodes, state, flag, s);
+    const uint32_t *perm_src = perms;
+    int mode = perm_mode;
+    if (perm_mode == NZ_PERM_MT19937) {
+        launch_mt_perms(M, n_runs, mt_seed_words, mt_seed_len, mt_words_stride, mt_perms, s);
+        perm_src = mt_perms;
+        mode = NZ_PERM_GIVEN;
+    }
+    UfParams p;
+    p.g = g;
+    p.n_runs = n_runs;
+    p.nodes = nodes;
+    p.state = state;
+    p.n_begin = 0;
+    p.n_end = M + 1;
+    p.key = key;
+    p.run0 = run0;
+    p.perms = perm_src;
+    p.rec = *out;
+    {
+        ProfScope prof(NZ_PROF_UNION_FIND, s);
+        launch_uf_window(p, mode, spanning != 0, n_runs >= 128 ? 128 : 32, s);
+    }
+    return check_launch();
+}
+
+void nz_profile_enable(int32_t enabled) {
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    g_prof.enabled = enabled != 0;
+}
+
+int nz_profile_read(int32_t n_categories, int64_t *launches, double *total_ms) {
+    if (n_categories <= 0 || !launches || !total_ms) return NZ_ERR_INVALID;
+    for (int i = 0; i < n_categories; ++i) { launches[i] = 0; total_ms[i] = 0.0; }
+    std::lock_guard<std::mutex> lk(g_prof.mu);
+    int status = NZ_OK;
+    for (auto &r : g_prof.recs) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&ms, r.a, r.b) != cudaSuccess)
+            status = NZ_ERR_CUDA;
+        if (r.cat >= 0 && r.cat < n_categories) { launches[r.cat] += 1; total_ms[r.cat] += ms; }
+        g_prof.pool.push_back(r.a);
+        g_prof.pool.push_back(r.b);
+    }
+    g_prof.recs.clear();
+    return status;
+}
+
+int nz_permutations(uint32_t num_edges, int32_t n_runs, int32_t perm_mode, uint64_t key, uint64_t run0,
+                    const uint32_t *mt_seed_words, const int32_t *mt_seed_len, int32_t mt_words_stride,
+                    uint32_t *out, void *stream) {
+    if (n_runs <= 0 || !out) return NZ_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    if (perm_mode == NZ_PERM_PHILOX) launch_philox_perms(num_edges, n_runs, key, run0, out, s);
+    else if (perm_mode == NZ_PERM_MT19937) {
+        if (!mt_seed_words || !mt_seed_len) return NZ_ERR_INVALID;
+        launch_mt_perms(num_edges, n_runs, mt_seed_words, mt_seed_len, mt_words_stride, out, s);
+    } else return NZ_ERR_INVALID;
+    return check_launch();
+}
+
+int nz_pack_microcanonical_rows(const NzRecords *rec, int32_t run, uint32_t num_nodes, uint32_t num_edges,
+                                int32_t spanning, uint8_t *rows, void *stream) {
+    if (!rec || !rows || run < 0 || !rec->max_span || !rec->m0 || !rec->m2 || !rec->m3 || !rec->m4_lo)
+        return NZ_ERR_INVALID;
+    launch_pack_rows(*rec, run, num_nodes, num_edges, spanning, rows, as_stream(stream));
+    return check_launch();
+}
+
+int32_t nz_binomial_band_cap(uint32_t num_edges, double cutoff) {
+    // Gaussian band half-width sqrt(2 cutoff) sigma with sigma <= sqrt(M)/2,
+    // widened by 25 % plus a margin for the skewed tails near p = 0, 1.
+    const double sigma = 0.5 * sqrt((double)num_edges);
+    double w = 2.0 * 1.25 * sqrt(2.0 * (cutoff > 0 ? cutoff : 0.0)) * sigma + 2.0 * cutoff + 64.0;
+    if (w > (double)num_edges + 1.0) w = (double)num_edges + 1.0;
+    return (int32_t)ceil(w);
+}
+
+int nz_binomial_weights(uint32_t num_edges, const double *ps, int32_t P, double cutoff, int32_t cap,
+                        uint32_t *band_lo, uint32_t *band_len, double *weights, void *stream) {
+    if (P <= 0 || !ps || !band_lo || !band_len || !weights || cap <= 0 || !(cutoff > 0)) return NZ_ERR_INVALID;
+    launch_binomial_weights(num_edges, ps, P, cutoff, cap, band_lo, band_len, weights, nullptr,
+                            as_stream(stream));
+    return check_launch();
+}
+
+int nz_binomial_pmf(uint32_t num_edges, const double *ps, int32_t P, double *out, void *stream) {
+    if (P <= 0 || !ps || !out) return NZ_ERR_INVALID;
+    launch_binomial_pmf(num_edges, ps, P, 745.0 /* FP64 underflow: the reference's own range */, out,
+                        as_stream(stream));
+    return check_launch();
+}
+
+int nz_canonical_statistics_rows(const uint8_t *rows, uint32_t num_edges, int32_t spanning, const double *factors,
+                                 int32_t n_factor_sets, double *out, void *stream) {
+    if (!rows || !factors || !out || n_factor_sets <= 0) return NZ_ERR_INVALID;
+    launch_canonical_rows(rows, num_edges, spanning, factors, n_factor_sets, out, as_stream(stream));
+    return check_launch();
+}
+
+int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, uint32_t num_edges, int32_t n_runs,
+                                    int32_t spanning, const uint32_t *band_lo, const uint32_t *band_len,
+                                    const double *weights, int32_t cap, int32_t P, double *out, void *stream) {
+    if (!rec || !band_lo || !band_len || !weights || !out || n_runs <= 0 || P <= 0) return NZ_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    if (cudaMemsetAsync(out, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess) return NZ_ERR_CUDA;
+    ConvParams p;
+    p.rec = *rec;
+    p.n_begin = 0;
+    p.n_end = num_edges + 1;
+    p.N = num_nodes;
+    p.n_runs = n_runs;
+    p.spanning = spanning;
+    p.P = P;
+    p.cap = cap;
+    p.band_lo = band_lo;
+    p.band_len = band_len;
+    p.w64 = weights;
+    p.w32 = nullptr;
+    p.acc = out;
+    launch_conv_window(p, 0, s);
+    return check_launch();
+}
+
+int nz_initialize_canonical_averages(const uint8_t *canonical_rows, int32_t P, int32_t spanning, uint8_t *out_rows,
+                                     void *stream) {
+    if (!canonical_rows || !out_rows || P < 0) return NZ_ERR_INVALID;
+    launch_init_avg(canonical_rows, P, spanning, out_rows, as_stream(stream));
+    return check_launch();
+}
+
+int nz_bond_reduce(const uint8_t *rows_a, const uint8_t *rows_b, int32_t P, int32_t spanning, uint8_t *out_rows,
+                   void *stream) {
+    if (!rows_a || !rows_b || !out_rows || P < 0) return NZ_ERR_INVALID;
+    launch_bond_reduce(rows_a, rows_b, P, spanning, out_rows, as_stream(stream));
+    return check_launch();
+}
+
+int nz_finalize_canonical_averages(const uint8_t *avg_rows, int32_t P, int32_t spanning, double number_of_nodes,
+                                   const double *ps, double alpha, uint8_t *out_rows, void *stream) {
+    if (!avg_rows || !out_rows || !ps || P < 0) return NZ_ERR_INVALID;
+    launch_finalize(avg_rows, P, spanning, number_of_nodes, ps, alpha, out_rows, as_stream(stream));
+    return check_launch();
+}
+
+int nz_microcanonical_finalize(const NzMicroAccum *acc, uint32_t num_nodes, uint32_t num_edges, int32_t spanning,
+                               double alpha, double *out, void *stream) {
+    if (!acc || !out || !acc->count || !acc->span_count || !acc->sum_lo || !acc->sum_hi || !acc->m2)
+        return NZ_ERR_INVALID;
+    if (!(alpha > 0.0 && alpha < 1.0)) return NZ_ERR_INVALID;
+    launch_micro_finalize(*acc, num_nodes, num_edges, spanning, alpha, out, as_stream(stream));
+    return check_launch();
+}
+
+int nz_student_t_quantile(const double *q, const double *df, int32_t count, double *out, void *stream) {
+    if (!q || !df || !out || count < 0) return NZ_ERR_INVALID;
+    launch_t_quantile(q, df, count, out, as_stream(stream));
+    return check_launch();
+}
+
+// ------------------------------------------------------------- ensemble
+namespace {
+
+struct EnsembleLayout {
+    uint32_t *nodes;
+    RunState *state;
+    uint32_t *flag;
+    NzRecords rec;
+    uint32_t *band_lo, *band_len;
+    double *w64;
+    float *w32;
+    double *stats;
+    double *part;
+    int32_t slices;
+    int32_t cap;
+    int32_t window;
+};
+
+constexpr double kDefaultCutoff = 80.0;
+
+int32_t pick_window(uint32_t M, int32_t n_runs, int32_t window) {
+    if (window > 0) return window > (int32_t)(M + 1) ? (int32_t)(M + 1) : window;
+    // records of one window at most ~8 GiB
+    double w = 8.0 * (1ull << 30) / ((double)n_runs * kRecordBytes);
+    if (w < 256) w = 256;
+    if (w > M + 1) w = M + 1;
+    return (int32_t)w;
+}
+
+size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, double cutoff, int32_t window,
+                       EnsembleLayout &L) {
+    L.window = pick_window(g.M, n_runs, window);
+    L.cap = nz_binomial_band_cap(g.M, cutoff);
+    L.nodes = c.take<uint32_t>((size_t)n_runs * g.N);
+    L.state = c.take<RunState>((size_t)n_runs);
+    L.flag = c.take<uint32_t>(4);
+    const size_t plane = (size_t)L.window * n_runs;
+    L.rec.max_span = c.take<uint32_t>(plane);
+    L.rec.m0 = c.take<uint32_t>(plane);
+    L.rec.m2 = c.take<uint64_t>(plane);
+    L.rec.m3 = c.take<uint64_t>(plane);
+    L.rec.m4_lo = c.take<uint64_t>(plane);
+    L.rec.m4_hi = c.take<uint32_t>(plane);
+    L.rec.edge = nullptr;
+    L.rec.run_stride = n_runs;
+    L.band_lo = c.take<uint32_t>(P);
+    L.band_len = c.take<uint32_t>(P);
+    L.w64 = c.take<double>((size_t)P * L.cap);
+    L.w32 = c.take<float>((size_t)P * L.cap);
+    L.stats = c.take<double>((size_t)n_runs * P * 7);
+    L.slices = n_runs < 1024 ? 1 : (n_runs < 65536 ? 16 : 64);
+    L.part = c.take<double>((size_t)L.slices * P * 7 * 3);
+    return c.used;
+}
+
+}  // namespace
+
+size_t nz_ensemble_workspace_bytes(const NzGraph *graph, int32_t n_runs, int32_t P, int32_t window) {
+    uint32_t N, M;
+    if (!graph || graph_size(*graph, N, M) != NZ_OK || n_runs <= 0 || P <= 0) return 0;
+    GraphDev g = make_graph_dev(*graph, N, M);
+    Carver c{nullptr, 0, 0};
+    EnsembleLayout L;
+    return align_up(ensemble_layout(c, g, n_runs, P, kDefaultCutoff, window, L));
+}
+
+int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t key, uint64_t run0,
+                const double *ps, int32_t P, double cutoff, int32_t window, int32_t conv_precision,
+                void *workspace, size_t workspace_bytes, uint64_t *acc_count, double *acc_mean, double *acc_m2,
+                const NzMicroAccum *micro, void *stream) {
+    if (!graph || n_runs <= 0 || P <= 0 || !ps || !acc_count || !acc_mean || !acc_m2) return NZ_ERR_INVALID;
+    if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
+    if (!(cutoff > 0)) cutoff = kDefaultCutoff;
+    if (cutoff > kDefaultCutoff) return NZ_ERR_INVALID;  // workspace is sized for the default band
+    if (conv_precision != 0 && conv_precision != 1) return NZ_ERR_INVALID;
+    uint32_t N, M;
+    int st = graph_size(*graph, N, M);
+    if (st) return st;
+    if (graph->kind == NZ_GRAPH_EDGES) return NZ_ERR_INVALID;  // lattices only on the fast path
+    if (micro && (!micro->count || !micro->span_count || !micro->sum_lo || !micro->sum_hi || !micro->m2))
+        return NZ_ERR_INVALID;
+    GraphDev g = make_graph_dev(*graph, N, M);
+    Carver c{static_cast<uint8_t *>(workspace), 0, workspace_bytes};
+    EnsembleLayout L;
+    ensemble_layout(c, g, n_runs, P, kDefaultCutoff, window, L);
+    if (!workspace || !c.ok()) return NZ_ERR_WORKSPACE;
+    cudaStream_t s = as_stream(stream);
+
+    {
+        ProfScope prof(NZ_PROF_SETUP, s);
+        launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
+        if (conv_precision == 1) launch_weights_to_f32(L.w64, L.w32, (size_t)P * L.cap, s);
+        launch_init_runs(g, n_runs, L.nodes, L.state, L.flag, s);
+        if (cudaMemsetAsync(L.stats, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess)
+            return NZ_ERR_CUDA;
+    }
+
+    UfParams up;
+    up.g = g;
+    up.n_runs = n_runs;
+    up.nodes = L.nodes;
+    up.state = L.state;
+    up.key = key;
+    up.run0 = run0;
+    up.perms = nullptr;
+    up.rec = L.rec;
+    ConvParams cp;
+    cp.rec = L.rec;
+    cp.N = N;
+    cp.n_runs = n_runs;
+    cp.spanning = spanning;
+    cp.P = P;
+    cp.cap = L.cap;
+    cp.band_lo = L.band_lo;
+    cp.band_len = L.band_len;
+    cp.w64 = L.w64;
+    cp.w32 = L.w32;
+    cp.acc = L.stats;
+    MicroParams mp;
+    if (micro) {
+        mp.rec = L.rec;
+        mp.N = N;
+        mp.n_runs = n_runs;
+        mp.acc = *micro;
+        mp.M = M;
+        mp.count_before = micro->count;
+    }
+    for (uint32_t w0 = 0; w0 <= M; w0 += (uint32_t)L.window) {
+        const uint32_t w1 = (w0 + (uint32_t)L.window > M + 1) ? M + 1 : w0 + (uint32_t)L.window;
+        up.n_begin = w0; up.n_end = w1;
+        {
+            ProfScope prof(NZ_PROF_UNION_FIND, s);
+            launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, 128, s);
+        }
+        if (micro) {
+            ProfScope prof(NZ_PROF_MICRO, s);
+            mp.n_begin = w0; mp.n_end = w1;
+            launch_micro_window(mp, s);
+        }
+        {
+            ProfScope prof(NZ_PROF_CONV, s);
+            cp.n_begin = w0; cp.n_end = w1;
+            launch_conv_window(cp, conv_precision, s);
+        }
+    }
+    {
+        ProfScope prof(NZ_PROF_REDUCE, s);
+        if (micro) launch_micro_count(micro->count, n_runs, s);
+        launch_reduce_runs(L.stats, n_runs, P, acc_count, acc_mean, acc_m2, L.part, L.slices, s);
+    }
+    return check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,697 @@
+// nz_canonical.cu -- canonical (binomial-convolution) stage, averages and
+// confidence intervals.
+//
+// Replaces percolate/percolate.py:1067-1109 (_binomial_pmf),
+// percolate/hpc.py:443-515 (bond_canonical_statistics), :561-635
+// (bond_initialize_canonical_averages), :638-702 (bond_reduce) and :752-834
+// (finalize_canonical_averages), plus the microcanonical run-reductions whose
+// semantics are percolate/percolate.py:450-705.
+#include <cmath>
+#include <cstdint>
+#include <type_traits>
+
+#include "nz_common.cuh"
+#include "nz_internal.cuh"
+#include "nz_math.cuh"
+
+namespace nz {
+
+// =====================================================================
+// Binomial weights
+// =====================================================================
+// Log B(M, n, p) up to an n-independent constant, from lgamma; used only to
+// locate the band edges (its absolute error does not reach the weights).
+__device__ __forceinline__ double log_binom_shape(uint32_t M, uint32_t n, double lp, double lq) {
+    return -lgamma((double)n + 1.0) - lgamma((double)(M - n) + 1.0) + (double)n * lp + (double)(M - n) * lq;
+}
+
+// One CTA per p.  Band = {n : log B(n) >= log B(mode) - cutoff}, found by
+// bisection on each side of the mode (log B is concave in n).  The weights
+// are then built from the ratio recursion of Newman & Ziff Eq. (10),
+//   log B(n) - log B(n-1) = log(M - n + 1) - log(n) + log(p) - log(1 - p),
+// summed by a block-wide prefix scan from the band's low edge, shifted by the
+// maximum, exponentiated and normalised by their FP64 sum (as the reference
+// normalises by ret.sum()).  Writes wp[0, cap) and returns (lo, len) to all
+// threads of the block.
+template <int BLOCK>
+__device__ void band_weights_block(uint32_t M, double p, double cutoff, int32_t cap, double *wp, uint32_t &lo_out,
+                                   uint32_t &len_out, bool &overflow) {
+    __shared__ double s_scan[BLOCK];
+    __shared__ double s_red[BLOCK];
+    __shared__ uint32_t s_lo, s_hi;
+    if (threadIdx.x == 0) {
+        uint32_t lo, hi;
+        if (!(p > 0.0)) { lo = hi = 0; }
+        else if (!(p < 1.0)) { lo = hi = M; }
+        else {
+            const double lp = log(p), lq = log1p(-p);
+            uint32_t mode = (uint32_t)floor((double)(M + 1) * p);
+            if (mode > M) mode = M;
+            const double lm = log_binom_shape(M, mode, lp, lq) - cutoff;
+            // smallest n <= mode with shape(n) >= lm
+            uint32_t a = 0, b = mode;
+            if (log_binom_shape(M, 0, lp, lq) >= lm) b = 0;
+            else while (b - a > 1) { uint32_t c = a + (b - a) / 2; if (log_binom_shape(M, c, lp, lq) >= lm) b = c; else a = c; }
+            lo = b;
+            // largest n >= mode with shape(n) >= lm
+            a = mode; b = M;
+            if (log_binom_shape(M, M, lp, lq) >= lm) a = M;
+            else while (b - a > 1) { uint32_t c = a + (b - a) / 2; if (log_binom_shape(M, c, lp, lq) >= lm) a = c; else b = c; }
+            hi = a;
+        }
+        s_lo = lo; s_hi = hi;
+    }
+    __syncthreads();
+    const uint32_t lo = s_lo;
+    uint32_t len = s_hi - s_lo + 1;
+    overflow = len > (uint32_t)cap;
+    if (overflow) len = cap;
+    lo_out = lo;
+    len_out = len;
+    if (len == 1) {
+        for (int j = threadIdx.x; j < cap; j += BLOCK) wp[j] = (j == 0) ? 1.0 : 0.0;
+        __syncthreads();
+        return;
+    }
+    const double lpq = log(p) - log1p(-p);
+    // pass 1: log weights relative to the low edge (prefix scan of log ratios)
+    double carry = 0.0;
+    double vmax = -INFINITY;
+    for (uint32_t base = 0; base < len; base += BLOCK) {
+        const uint32_t j = base + threadIdx.x;
+        double x = 0.0;
+        if (j > 0 && j < len) {
+            const double n = (double)(lo + j);
+            x = log((double)M - n + 1.0) - log(n) + lpq;
+        }
+        s_scan[threadIdx.x] = x;
+        __syncthreads();
+        for (int off = 1; off < BLOCK; off <<= 1) {  // Hillis-Steele inclusive scan
+            double y = threadIdx.x >= (unsigned)off ? s_scan[threadIdx.x - off] : 0.0;
+            __syncthreads();
+            s_scan[threadIdx.x] += y;
+            __syncthreads();
+        }
+        const double lv = carry + s_scan[threadIdx.x];
+        if (j < len) { wp[j] = lv; vmax = fmax(vmax, lv); }
+        carry += s_scan[BLOCK - 1];
+        __syncthreads();
+    }
+    s_red[threadIdx.x] = vmax;
+    __syncthreads();
+    for (int off = BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < (unsigned)off) s_red[threadIdx.x] = fmax(s_red[threadIdx.x], s_red[threadIdx.x + off]);
+        __syncthreads();
+    }
+    vmax = s_red[0];
+    __syncthreads();
+    // pass 2: exponentiate and sum
+    double sum = 0.0;
+    for (uint32_t j = threadIdx.x; j < len; j += BLOCK) {
+        const double e = exp(wp[j] - vmax);
+        wp[j] = e;
+        sum += e;
+    }
+    s_red[threadIdx.x] = sum;
+    __syncthreads();
+    for (int off = BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < (unsigned)off) s_red[threadIdx.x] += s_red[threadIdx.x + off];
+        __syncthreads();
+    }
+    const double inv = 1.0 / s_red[0];
+    for (uint32_t j = threadIdx.x; j < (uint32_t)cap; j += BLOCK) wp[j] = (j < len) ? wp[j] * inv : 0.0;
+    __syncthreads();
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) binomial_weights_kernel(uint32_t M, const double *ps, double cutoff,
+                                                                 int32_t cap, uint32_t *band_lo,
+                                                                 uint32_t *band_len, double *w,
+                                                                 int32_t *overflow) {
+    const int pi = blockIdx.x;
+    uint32_t lo, len;
+    bool ovf;
+    band_weights_block<BLOCK>(M, ps[pi], cutoff, cap, w + (size_t)pi * cap, lo, len, ovf);
+    if (threadIdx.x == 0) {
+        band_lo[pi] = lo;
+        band_len[pi] = len;
+        if (ovf && overflow) atomicExch(overflow, 1);
+    }
+}
+
+// Full-length pmf rows out[pi][0..M]: band weights computed at the row start,
+// then shifted in place to their offset and the rest zeroed.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) binomial_pmf_kernel(uint32_t M, const double *ps, double cutoff,
+                                                             double *out) {
+    const int pi = blockIdx.x;
+    double *row = out + (size_t)pi * (M + 1);
+    uint32_t lo, len;
+    bool ovf;
+    band_weights_block<BLOCK>(M, ps[pi], cutoff, (int32_t)(M + 1), row, lo, len, ovf);
+    if (lo > 0) {
+        // move [0, len) to [lo, lo + len), highest block first
+        for (int64_t top = (int64_t)len; top > 0; top -= BLOCK) {
+            const int64_t j = top - BLOCK + threadIdx.x;
+            double v = 0.0;
+            if (j >= 0) v = row[j];
+            __syncthreads();
+            if (j >= 0) row[j + lo] = v;
+            __syncthreads();
+        }
+        for (uint32_t j = threadIdx.x; j < lo; j += BLOCK) row[j] = 0.0;
+    }
+}
+
+void launch_binomial_weights(uint32_t M, const double *ps, int32_t P, double cutoff, int32_t cap,
+                             uint32_t *band_lo, uint32_t *band_len, double *w, int32_t *overflow,
+                             cudaStream_t s) {
+    if (P <= 0) return;
+    binomial_weights_kernel<256><<<P, 256, 0, s>>>(M, ps, cutoff, cap, band_lo, band_len, w, overflow);
+}
+
+void launch_binomial_pmf(uint32_t M, const double *ps, int32_t P, double cutoff, double *out, cudaStream_t s) {
+    if (P <= 0) return;
+    binomial_pmf_kernel<256><<<P, 256, 0, s>>>(M, ps, cutoff, out);
+}
+
+// =====================================================================
+// bond_canonical_statistics on the reference's packed rows (FP64)
+// =====================================================================
+__device__ __forceinline__ uint64_t ld_bytes(const uint8_t *p, int n) {
+    uint64_t v = 0;
+    for (int i = 0; i < n; ++i) v |= (uint64_t)p[i] << (8 * i);
+    return v;
+}
+
+// grid: (factor set); each CTA reduces over the M+1 rows.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) canonical_rows_kernel(const uint8_t *rows, uint32_t M, int32_t spanning,
+                                                               const double *factors, double *out) {
+    const int set = blockIdx.x;
+    const double *f = factors + (size_t)set * (M + 1);
+    const uint32_t rb = spanning ? 53u : 52u;
+    const int o = spanning ? 9 : 8;
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (uint32_t n = threadIdx.x; n <= M; n += BLOCK) {
+        const uint8_t *r = rows + (size_t)n * rb;
+        const double fn = f[n];
+        if (spanning) acc[0] += fn * (double)(r[8] != 0);
+        acc[1] += fn * (double)(uint32_t)ld_bytes(r + o, 4);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) acc[2 + k] += fn * (double)ld_bytes(r + o + 4 + 8 * k, 8);
+    }
+    __shared__ double s_red[7][BLOCK];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) s_red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int off = BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < (unsigned)off)
+#pragma unroll
+            for (int k = 0; k < 7; ++k) s_red[k][threadIdx.x] += s_red[k][threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x < 7) out[(size_t)set * 7 + threadIdx.x] = (threadIdx.x == 0 && !spanning) ? 0.0 : s_red[threadIdx.x][0];
+}
+
+void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, const double *factors,
+                           int32_t n_sets, double *out, cudaStream_t s) {
+    if (n_sets <= 0) return;
+    canonical_rows_kernel<256><<<n_sets, 256, 0, s>>>(rows, M, spanning, factors, out);
+}
+
+// =====================================================================
+// Banded convolution of record windows (ensemble path)
+// =====================================================================
+// Statistic s of run r at row n (record planes of the window).
+__device__ __forceinline__ double record_value(const NzRecords &rec, size_t off, int s, uint32_t N) {
+    switch (s) {
+        case 0: return (rec.max_span[off] & kSpanBit) ? 1.0 : 0.0;
+        case 1: return (double)(rec.max_span[off] & ~kSpanBit);
+        case 2: return (double)rec.m0[off];
+        case 3: return (double)(N - (rec.max_span[off] & ~kSpanBit));
+        case 4: return (double)rec.m2[off];
+        case 5: return (double)rec.m3[off];
+        default: return ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off];
+    }
+}
+
+__device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off, int s, uint32_t N) {
+    switch (s) {
+        case 0: return (rec.max_span[off] & kSpanBit) ? 1.0f : 0.0f;
+        case 1: return (float)(rec.max_span[off] & ~kSpanBit);
+        case 2: return (float)rec.m0[off];
+        case 3: return (float)(N - (rec.max_span[off] & ~kSpanBit));
+        case 4: return __ull2float_rn(rec.m2[off]);
+        case 5: return __ull2float_rn(rec.m3[off]);
+        default: return (float)(ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off]);
+    }
+}
+
+constexpr int kConvRuns = 128;  // runs per CTA (one per thread)
+constexpr int kConvPT = 16;     // probabilities per CTA
+constexpr int kConvChunk = 64;  // rows staged per step
+
+// grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
+// kConvPT canonical values of its run for one statistic over the window's
+// rows, with the tile's weights staged in shared memory (zero outside each
+// p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
+// products summed in FP32 over kConvChunk rows, then added into FP64.
+template <int PRECISION>
+__global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
+    using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
+    __shared__ wtype s_w[kConvChunk][kConvPT];
+    __shared__ uint32_t s_lo[kConvPT], s_len[kConvPT];
+    __shared__ uint32_t s_range[2];
+    const int r = blockIdx.x * kConvRuns + threadIdx.x;
+    const int p0 = blockIdx.y * kConvPT;
+    const int s = blockIdx.z;
+    if (s == 0 && !p.spanning) return;
+    if (threadIdx.x < kConvPT) {
+        const int pi = p0 + threadIdx.x;
+        s_lo[threadIdx.x] = pi < p.P ? p.band_lo[pi] : 0u;
+        s_len[threadIdx.x] = pi < p.P ? p.band_len[pi] : 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t a = 0xffffffffu, b = 0;
+        for (int j = 0; j < kConvPT; ++j)
+            if (s_len[j]) { a = min(a, s_lo[j]); b = max(b, s_lo[j] + s_len[j]); }
+        a = max(a, p.n_begin);
+        b = min(b, p.n_end);
+        s_range[0] = a; s_range[1] = b;
+    }
+    __syncthreads();
+    const uint32_t nlo = s_range[0], nhi = s_range[1];
+    if (nlo >= nhi) return;
+    double acc[kConvPT];
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) acc[j] = 0.0;
+    for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
+        const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < kConvChunk * kConvPT; i += kConvRuns) {
+            const int row = i / kConvPT, j = i % kConvPT;
+            const uint32_t n = c0 + row;
+            wtype v = 0;
+            if (row < (int)cn && n >= s_lo[j] && n < s_lo[j] + s_len[j]) {
+                const size_t widx = (size_t)(p0 + j) * p.cap + (n - s_lo[j]);
+                v = PRECISION == 0 ? (wtype)p.w64[widx] : (wtype)p.w32[widx];
+            }
+            s_w[row][j] = v;
+        }
+        __syncthreads();
+        if (r < p.n_runs) {
+            wtype part[kConvPT];
+#pragma unroll
+            for (int j = 0; j < kConvPT; ++j) part[j] = 0;
+            for (uint32_t i = 0; i < cn; ++i) {
+                const size_t off = (size_t)(c0 + i - p.n_begin) * p.rec.run_stride + r;
+                const wtype q = PRECISION == 0 ? (wtype)record_value(p.rec, off, s, p.N)
+                                               : (wtype)record_value_f(p.rec, off, s, p.N);
+#pragma unroll
+                for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
+        }
+    }
+    if (r < p.n_runs) {
+#pragma unroll
+        for (int j = 0; j < kConvPT; ++j) {
+            const int pi = p0 + j;
+            if (pi < p.P) p.acc[((size_t)r * p.P + pi) * 7 + s] += acc[j];
+        }
+    }
+}
+
+void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
+    if (p.n_runs <= 0 || p.P <= 0) return;
+    dim3 grid((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 7);
+    if (precision == 0) conv_window_kernel<0><<<grid, kConvRuns, 0, s>>>(p);
+    else conv_window_kernel<1><<<grid, kConvRuns, 0, s>>>(p);
+}
+
+__global__ void f64_to_f32_kernel(const double *a, float *b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+void launch_weights_to_f32(const double *w64, float *w32, size_t count, cudaStream_t s) {
+    if (!count) return;
+    size_t blocks = (count + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(w64, w32, count);
+}
+
+// =====================================================================
+// Pairwise (n, mean, M2) reduction over runs
+// =====================================================================
+// Chan, Golub & LeVeque (1979) pairwise update, the formula simoa's
+// online_variance applies in bond_reduce (percolate/hpc.py:674-692).
+__device__ __forceinline__ void chan_merge(double &na, double &ma, double &sa, double nb, double mb, double sb) {
+    if (nb == 0.0) return;
+    if (na == 0.0) { na = nb; ma = mb; sa = sb; return; }
+    const double n = na + nb;
+    const double d = mb - ma;
+    ma += d * nb / n;
+    sa += sb + d * d * na * nb / n;
+    na = n;
+}
+
+// stats [n_runs][P*7]: one thread per column, looping over a slice of runs;
+// partial (n, mean, M2) go to `part` [slices][cols][3].
+__global__ void reduce_runs_partial_kernel(const double *stats, int32_t n_runs, int32_t cols, int32_t slice,
+                                           double *part) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sl = blockIdx.y;
+    if (c >= cols) return;
+    const int r0 = sl * slice, r1 = min(n_runs, r0 + slice);
+    double n = 0, mean = 0, m2 = 0;
+    for (int r = r0; r < r1; ++r) {  // Welford == merging (1, x, 0)
+        const double x = stats[(size_t)r * cols + c];
+        n += 1.0;
+        const double d = x - mean;
+        mean += d / n;
+        m2 += d * (x - mean);
+    }
+    double *o = part + ((size_t)sl * cols + c) * 3;
+    o[0] = n; o[1] = mean; o[2] = m2;
+}
+
+__global__ void reduce_runs_final_kernel(const double *part, int32_t cols, int32_t slices, const uint64_t *acc_count,
+                                         double *acc_mean, double *acc_m2) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    double n = 0, mean = 0, m2 = 0;
+    for (int sl = 0; sl < slices; ++sl) {
+        const double *o = part + ((size_t)sl * cols + c) * 3;
+        chan_merge(n, mean, m2, o[0], o[1], o[2]);
+    }
+    double na = (double)*acc_count, ma = acc_mean[c], sa = acc_m2[c];
+    chan_merge(na, ma, sa, n, mean, m2);
+    acc_mean[c] = ma;
+    acc_m2[c] = sa;
+}
+
+__global__ void add_count_kernel(uint64_t *count, int32_t n) { *count += (uint64_t)n; }
+
+void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t *acc_count, double *acc_mean,
+                           double *acc_m2, double *part, int32_t slices, cudaStream_t s) {
+    const int cols = P * 7;
+    const int slice = (n_runs + slices - 1) / slices;
+    dim3 grid((cols + 127) / 128, slices);
+    reduce_runs_partial_kernel<<<grid, 128, 0, s>>>(stats, n_runs, cols, slice, part);
+    reduce_runs_final_kernel<<<(cols + 127) / 128, 128, 0, s>>>(part, cols, slices, acc_count, acc_mean, acc_m2);
+    add_count_kernel<<<1, 1, 0, s>>>(acc_count, n_runs);
+}
+
+// =====================================================================
+// Microcanonical run-reductions (fused over a window of records)
+// =====================================================================
+// Per (row n, statistic): exact integer sum over runs and the sum of squared
+// deviations, merged into the accumulators with the pairwise formula.
+// Statistics: 0 max, 1 m0, 2 m1 (= N - max), 3 m2, 4 m3, 5 m4; plus the
+// count of spanning runs.  Squares are taken of the deviation from run 0's
+// value (an exact 128-bit integer, converted to FP64), which keeps the FP64
+// sum free of cancellation.
+__device__ __forceinline__ void record_u128(const NzRecords &rec, size_t off, int s, uint32_t N, uint64_t &lo,
+                                            uint64_t &hi) {
+    hi = 0;
+    switch (s) {
+        case 0: lo = rec.max_span[off] & ~kSpanBit; break;
+        case 1: lo = rec.m0[off]; break;
+        case 2: lo = N - (rec.max_span[off] & ~kSpanBit); break;
+        case 3: lo = rec.m2[off]; break;
+        case 4: lo = rec.m3[off]; break;
+        default: lo = rec.m4_lo[off]; hi = rec.m4_hi[off]; break;
+    }
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
+    const uint32_t n = p.n_begin + blockIdx.x;
+    const int s = blockIdx.y;  // 0..5 statistics, 6 = spanning count
+    const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;
+    __shared__ uint64_t s_lo[BLOCK], s_hi[BLOCK], s_cnt[BLOCK];
+    __shared__ double s_sq[BLOCK];
+    __shared__ double s_d[BLOCK];
+    if (s == 6) {
+        uint64_t c = 0;
+        for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) c += (p.rec.max_span[row + r] & kSpanBit) ? 1u : 0u;
+        s_cnt[threadIdx.x] = c;
+        __syncthreads();
+        for (int off = BLOCK / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < (unsigned)off) s_cnt[threadIdx.x] += s_cnt[threadIdx.x + off];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) p.acc.span_count[n] += s_cnt[0];
+        return;
+    }
+    uint64_t x0lo, x0hi;
+    record_u128(p.rec, row, s, p.N, x0lo, x0hi);
+    uint64_t slo = 0, shi = 0;  // exact sum (unsigned 128)
+    double sd = 0.0, sq = 0.0;  // sum of deviations and squared deviations
+    for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
+        uint64_t lo, hi;
+        record_u128(p.rec, row + r, s, p.N, lo, hi);
+        uint64_t nlo = slo + lo;
+        shi += hi + (nlo < slo ? 1ull : 0ull);
+        slo = nlo;
+        // deviation from run 0 as a signed 128-bit value -> double
+        uint64_t dlo = lo - x0lo;
+        uint64_t dhi = hi - x0hi - (lo < x0lo ? 1ull : 0ull);
+        double d;
+        if ((int64_t)dhi < 0) {  // negative: negate
+            uint64_t nlo2 = ~dlo + 1ull;
+            uint64_t nhi2 = ~dhi + (nlo2 == 0 ? 1ull : 0ull);
+            d = -(ldexp((double)nhi2, 64) + (double)nlo2);
+        } else {
+            d = ldexp((double)dhi, 64) + (double)dlo;
+        }
+        sd += d;
+        sq = fma(d, d, sq);
+    }
+    s_lo[threadIdx.x] = slo; s_hi[threadIdx.x] = shi; s_sq[threadIdx.x] = sq; s_d[threadIdx.x] = sd;
+    __syncthreads();
+    for (int off = BLOCK / 2; off > 0; off >>= 1) {
+        if (threadIdx.x < (unsigned)off) {
+            uint64_t a = s_lo[threadIdx.x], b = s_lo[threadIdx.x + off];
+            uint64_t nlo = a + b;
+            s_hi[threadIdx.x] += s_hi[threadIdx.x + off] + (nlo < a ? 1ull : 0ull);
+            s_lo[threadIdx.x] = nlo;
+            s_sq[threadIdx.x] += s_sq[threadIdx.x + off];
+            s_d[threadIdx.x] += s_d[threadIdx.x + off];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double R = (double)p.n_runs;
+        const double sumd = s_d[0];
+        double m2b = s_sq[0] - sumd * sumd / R;
+        if (m2b < 0.0) m2b = 0.0;
+        const double mean_b = (ldexp((double)s_hi[0], 64) + (double)s_lo[0]) / R;
+        const size_t idx = (size_t)s * (p.M + 1) + n;
+        const double na = (double)*p.count_before;
+        const uint64_t alo = p.acc.sum_lo[idx], ahi = p.acc.sum_hi[idx];
+        const double mean_a = na > 0 ? (ldexp((double)ahi, 64) + (double)alo) / na : 0.0;
+        double nn = na, mm = mean_a, ss = p.acc.m2[idx];
+        chan_merge(nn, mm, ss, R, mean_b, m2b);
+        uint64_t nlo = alo + s_lo[0];
+        p.acc.sum_hi[idx] = ahi + s_hi[0] + (nlo < alo ? 1ull : 0ull);
+        p.acc.sum_lo[idx] = nlo;
+        p.acc.m2[idx] = ss;
+    }
+}
+
+void launch_micro_window(const MicroParams &p, cudaStream_t s) {
+    dim3 grid(p.n_end - p.n_begin, 7);
+    if (grid.x == 0 || p.n_runs <= 0) return;
+    micro_window_kernel<256><<<grid, 256, 0, s>>>(p);
+}
+
+void launch_micro_count(uint64_t *count, int32_t n_runs, cudaStream_t s) {
+    add_count_kernel<<<1, 1, 0, s>>>(count, n_runs);
+}
+
+// =====================================================================
+// Row-format kernels: initialize / reduce / finalize
+// =====================================================================
+// Packed structured rows with 4-byte alignment: doubles are moved as two words.
+__device__ __forceinline__ double ld_f64(const uint8_t *p) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(p);
+    return __hiloint2double((int)w[1], (int)w[0]);
+}
+__device__ __forceinline__ void st_f64(uint8_t *p, double v) {
+    uint32_t *w = reinterpret_cast<uint32_t *>(p);
+    w[0] = (uint32_t)__double2loint(v);
+    w[1] = (uint32_t)__double2hiint(v);
+}
+
+// canonical_statistics_dtype (hpc.py:407-440): [pp f8] max f8 moments 5*f8
+// canonical_averages_dtype  (hpc.py:518-558): n u4 [pp_mean pp_m2] max_mean max_m2
+//                                             moments_mean 5*f8 moments_m2 5*f8
+__global__ void init_avg_kernel(const uint8_t *canon, int32_t P, int32_t spanning, uint8_t *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int nst = spanning ? 7 : 6;
+    const uint8_t *c = canon + (size_t)i * nst * 8;
+    uint8_t *o = out + (size_t)i * (4 + nst * 16);
+    *reinterpret_cast<uint32_t *>(o) = 1u;
+    int k = 0;
+    if (spanning) { st_f64(o + 4, ld_f64(c)); st_f64(o + 12, 0.0); k = 1; }
+    const int base = 4 + k * 16;
+    st_f64(o + base, ld_f64(c + k * 8));
+    st_f64(o + base + 8, 0.0);
+    for (int m = 0; m < 5; ++m) {
+        st_f64(o + base + 16 + 8 * m, ld_f64(c + (k + 1 + m) * 8));
+        st_f64(o + base + 56 + 8 * m, 0.0);
+    }
+}
+
+void launch_init_avg(const uint8_t *canon_rows, int32_t P, int32_t spanning, uint8_t *out, cudaStream_t s) {
+    if (P > 0) init_avg_kernel<<<(P + 127) / 128, 128, 0, s>>>(canon_rows, P, spanning, out);
+}
+
+__global__ void bond_reduce_kernel(const uint8_t *a, const uint8_t *b, int32_t P, int32_t spanning, uint8_t *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int nst = spanning ? 7 : 6;
+    const size_t rb = 4 + nst * 16;
+    const uint8_t *ra = a + i * rb, *rbp = b + i * rb;
+    uint8_t *o = out + i * rb;
+    const uint32_t na = *reinterpret_cast<const uint32_t *>(ra);
+    const uint32_t nb = *reinterpret_cast<const uint32_t *>(rbp);
+    // (mean offset, m2 offset) pairs
+    int mo[7], so[7], cnt = 0;
+    int off = 4;
+    if (spanning) { mo[cnt] = off; so[cnt] = off + 8; ++cnt; off += 16; }
+    mo[cnt] = off; so[cnt] = off + 8; ++cnt; off += 16;
+    for (int m = 0; m < 5; ++m) { mo[cnt] = off + 8 * m; so[cnt] = off + 40 + 8 * m; ++cnt; }
+    for (int k = 0; k < cnt; ++k) {
+        double n1 = (double)na, m1 = ld_f64(ra + mo[k]), s1 = ld_f64(ra + so[k]);
+        const double n2 = (double)nb, m2 = ld_f64(rbp + mo[k]), s2 = ld_f64(rbp + so[k]);
+        const double n = n1 + n2;
+        const double d = m2 - m1;
+        const double mean = m1 + d * n2 / n;
+        const double ss = s1 + s2 + d * d * n1 * n2 / n;
+        st_f64(o + mo[k], mean);
+        st_f64(o + so[k], ss);
+    }
+    *reinterpret_cast<uint32_t *>(o) = na + nb;
+}
+
+void launch_bond_reduce(const uint8_t *a, const uint8_t *b, int32_t P, int32_t spanning, uint8_t *out,
+                        cudaStream_t s) {
+    if (P > 0) bond_reduce_kernel<<<(P + 127) / 128, 128, 0, s>>>(a, b, P, spanning, out);
+}
+
+// finalized_canonical_averages_dtype (hpc.py:705-749):
+//   n u4, p f8, alpha f8, [pp_mean, pp_std, pp_ci 2*f8], strength_mean, strength_std,
+//   strength_ci 2*f8, moments_mean 5*f8, moments_std 5*f8, moments_ci 5*2*f8
+__device__ void t_interval(double conf, double df, double loc, double scale, double &lo, double &hi) {
+    // scipy.stats.t.interval: ppf((1 - conf)/2), ppf((1 + conf)/2); NaN unless
+    // scale > 0 and df > 0.
+    if (!(scale > 0.0) || !(df > 0.0) || isnan(loc)) { lo = NAN; hi = NAN; return; }
+    const double qa = (1.0 - conf) / 2.0, qb = (1.0 + conf) / 2.0;
+    lo = loc + scale * student_t_quantile(qa, df);
+    hi = loc + scale * student_t_quantile(qb, df);
+}
+
+__global__ void finalize_kernel(const uint8_t *avg, int32_t P, int32_t spanning, double N, const double *ps,
+                                double alpha, uint8_t *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const int nst = spanning ? 7 : 6;
+    const uint8_t *a = avg + (size_t)i * (4 + nst * 16);
+    uint8_t *o = out + (size_t)i * (spanning ? 244 : 212);
+    const uint32_t nu = *reinterpret_cast<const uint32_t *>(a);
+    const double n = (double)nu;
+    const double nm1 = (double)(uint32_t)(nu - 1u);  // numpy uint32 arithmetic
+    const double sqrt_n = sqrt(n);
+    const double conf = 1.0 - alpha;
+    *reinterpret_cast<uint32_t *>(o) = nu;
+    st_f64(o + 4, ps[i]);
+    st_f64(o + 12, alpha);
+    int ai = 4, oi = 20;
+    auto transform = [&](double mean, double m2, bool normalize, uint8_t *pm, uint8_t *pstd, uint8_t *pci) {
+        double mu = mean, sd = sqrt(m2 / nm1);
+        if (normalize) { mu /= N; sd /= N; }
+        st_f64(pm, mu);
+        st_f64(pstd, sd);
+        double lo, hi;
+        t_interval(conf, nm1, mu, sd / sqrt_n, lo, hi);
+        st_f64(pci, lo);
+        st_f64(pci + 8, hi);
+    };
+    if (spanning) {
+        transform(ld_f64(a + ai), ld_f64(a + ai + 8), false, o + oi, o + oi + 8, o + oi + 16);
+        ai += 16; oi += 32;
+    }
+    transform(ld_f64(a + ai), ld_f64(a + ai + 8), true, o + oi, o + oi + 8, o + oi + 16);
+    ai += 16; oi += 32;
+    for (int m = 0; m < 5; ++m)
+        transform(ld_f64(a + ai + 8 * m), ld_f64(a + ai + 40 + 8 * m), true, o + oi + 8 * m, o + oi + 40 + 8 * m,
+                  o + oi + 80 + 16 * m);
+}
+
+void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, const double *ps, double alpha,
+                     uint8_t *out, cudaStream_t s) {
+    if (P > 0) finalize_kernel<<<(P + 63) / 64, 64, 0, s>>>(avg, P, spanning, N, ps, alpha, out);
+}
+
+// Microcanonical averages from the run-reduction accumulators, per row n
+// (percolate/percolate.py:450-705 and :968-1064): spanning -> Bayesian
+// posterior mean (k+1)/(R+2) with Beta(k+1, R-k+1) quantiles at alpha/2 and
+// 1 - alpha/2; max and moments -> mean and Student-t interval with scale
+// std/sqrt(R), std with ddof 1, (mean, mean) where std == 0; max and moments
+// divided by N as microcanonical_averages_arrays returns them.
+// out[n * 21 + ...]: span (mean, lo, hi), max (mean, lo, hi), m0..m4 (mean, lo, hi).
+__global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
+                                      double *out) {
+    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n > M) return;
+    const double R = (double)*acc.count;
+    double *o = out + (size_t)n * 21;
+    if (spanning) {
+        const double k = (double)acc.span_count[n];
+        o[0] = (k + 1.0) / (R + 2.0);
+        o[1] = beta_quantile(alpha / 2.0, k + 1.0, R - k + 1.0);
+        o[2] = beta_quantile(1.0 - alpha / 2.0, k + 1.0, R - k + 1.0);
+    } else {
+        o[0] = o[1] = o[2] = NAN;
+    }
+    const int map[6] = {0, 1, 2, 3, 4, 5};  // max, m0, m1, m2, m3, m4
+    for (int j = 0; j < 6; ++j) {
+        const size_t idx = (size_t)map[j] * (M + 1) + n;
+        const double mean = (ldexp((double)acc.sum_hi[idx], 64) + (double)acc.sum_lo[idx]) / R;
+        const double m2 = acc.m2[idx];
+        const double sd = R > 1.0 ? sqrt(m2 / (R - 1.0)) : NAN;
+        double lo = mean, hi = mean;
+        if (sd > 0.0) {
+            const double conf = 1.0 - alpha;
+            const double sc = sd / sqrt(R);
+            lo = mean + sc * student_t_quantile((1.0 - conf) / 2.0, R - 1.0);
+            hi = mean + sc * student_t_quantile((1.0 + conf) / 2.0, R - 1.0);
+        }
+        o[3 + 3 * j] = mean / N;
+        o[4 + 3 * j] = lo / N;
+        o[5 + 3 * j] = hi / N;
+    }
+}
+
+void launch_micro_finalize(const NzMicroAccum &acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
+                           double *out, cudaStream_t s) {
+    micro_finalize_kernel<<<(M + 1 + 127) / 128, 128, 0, s>>>(acc, N, M, spanning, alpha, out);
+}
+
+__global__ void t_quantile_kernel(const double *q, const double *df, int32_t count, double *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = student_t_quantile(q[i], df[i]);
+}
+
+void launch_t_quantile(const double *q, const double *df, int32_t count, double *out, cudaStream_t s) {
+    if (count > 0) t_quantile_kernel<<<(count + 127) / 128, 128, 0, s>>>(q, df, count, out);
+}
+
+}  // namespace nz

@@ -1,0 +1,83 @@
+// nz_internal.cuh -- kernel parameter blocks and launcher declarations shared
+// between the translation units of libnzgb300.so (not part of the C ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nz_common.cuh"
+
+namespace nz {
+
+struct UfParams {
+    GraphDev g;
+    int32_t n_runs;
+    uint32_t *nodes;        // [n_runs][N]
+    RunState *state;        // [n_runs]
+    uint32_t n_begin;       // rows emitted: [n_begin, n_end)
+    uint32_t n_end;
+    uint64_t key, run0;     // NZ_PERM_PHILOX
+    const uint32_t *perms;  // [n_runs][M] otherwise
+    NzRecords rec;          // row n of run r at plane[(n - n_begin) * run_stride + r]
+};
+
+// nz_uf.cu
+void launch_init_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,
+                      uint32_t *flag_scratch, cudaStream_t s);
+void launch_uf_window(const UfParams &p, int perm_mode, bool span, int block, cudaStream_t s);
+void launch_philox_perms(uint32_t M, int32_t n_runs, uint64_t key, uint64_t run0, uint32_t *out,
+                         cudaStream_t s);
+void launch_mt_perms(uint32_t M, int32_t n_runs, const uint32_t *seed_words, const int32_t *seed_len,
+                     int32_t stride, uint32_t *out, cudaStream_t s);
+void launch_pack_rows(const NzRecords &rec, int32_t run, uint32_t N, uint32_t M, int32_t spanning,
+                      uint8_t *rows, cudaStream_t s);
+
+// nz_canonical.cu
+void launch_binomial_weights(uint32_t M, const double *ps, int32_t P, double cutoff, int32_t cap,
+                             uint32_t *band_lo, uint32_t *band_len, double *w, int32_t *overflow,
+                             cudaStream_t s);
+void launch_binomial_pmf(uint32_t M, const double *ps, int32_t P, double cutoff, double *out, cudaStream_t s);
+void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, const double *factors,
+                           int32_t n_sets, double *out, cudaStream_t s);
+
+struct ConvParams {
+    NzRecords rec;           // window records, row n at (n - n_begin)
+    uint32_t n_begin, n_end; // window rows
+    uint32_t N;
+    int32_t n_runs;
+    int32_t spanning;
+    int32_t P, cap;
+    const uint32_t *band_lo, *band_len;
+    const double *w64;       // [P][cap]
+    const float *w32;        // [P][cap] (FP32 path)
+    double *acc;             // [n_runs][P][7], accumulated (+=)
+};
+void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s);
+void launch_weights_to_f32(const double *w64, float *w32, size_t count, cudaStream_t s);
+// part: scratch [slices][P*7][3] doubles
+void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t *acc_count,
+                        double *acc_mean, double *acc_m2, double *part, int32_t slices, cudaStream_t s);
+
+struct MicroParams {
+    NzRecords rec;
+    uint32_t n_begin, n_end;
+    uint32_t N;
+    int32_t n_runs;
+    NzMicroAccum acc;
+    uint32_t M;
+    const uint64_t *count_before;  // device: runs already in acc
+};
+void launch_micro_window(const MicroParams &p, cudaStream_t s);
+void launch_micro_count(uint64_t *count, int32_t n_runs, cudaStream_t s);
+
+void launch_init_avg(const uint8_t *canon_rows, int32_t P, int32_t spanning, uint8_t *out, cudaStream_t s);
+void launch_bond_reduce(const uint8_t *a, const uint8_t *b, int32_t P, int32_t spanning, uint8_t *out,
+                        cudaStream_t s);
+void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, const double *ps,
+                     double alpha, uint8_t *out, cudaStream_t s);
+void launch_micro_finalize(const NzMicroAccum &acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
+                           double *out, cudaStream_t s);
+void launch_t_quantile(const double *q, const double *df, int32_t count, double *out, cudaStream_t s);
+
+}  // namespace nz

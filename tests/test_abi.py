@@ -1,0 +1,124 @@
+"""CPU checks of the C ABI library and the host-side logic (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def _declared_functions():
+    src = open(os.path.join(REPO, 'include', 'nz_gb300.h')).read()
+    src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
+    names = re.findall(r'\b(nz_[a-z0-9_]+)\s*\(', src)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from pypercolate_gb300 import build
+    build.build()
+    return ctypes.CDLL(build.LIB)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+def test_bindings_cover_header():
+    from pypercolate_gb300 import _native
+    assert set(_declared_functions()) == set(_native.EXPORTED)
+
+
+def test_host_only_entry_points(lib):
+    from pypercolate_gb300 import _native as nat
+    L = nat.lib_handle()
+    assert b'sm_103a' in L.nz_version()
+    assert nat.graph_size(nat.make_graph(nat.GRAPH_GRID2D, 256)) == (65536, 130560)
+    assert nat.graph_size(nat.make_graph(nat.GRAPH_CHAIN1D, 1)) == (1, 0)
+    with pytest.raises(ValueError):
+        nat.graph_size(nat.make_graph(nat.GRAPH_CHAIN1D, 0))
+    with pytest.raises(nat.NzError):
+        nat.graph_size(nat.make_graph(nat.GRAPH_GRID2D, 2048))
+    g = nat.make_graph(nat.GRAPH_GRID2D, 256)
+    assert L.nz_microcanonical_workspace_bytes(g, 10, nat.PERM_PHILOX) >= 10 * 65536 * 4
+    assert L.nz_ensemble_workspace_bytes(g, 100, 1001, 0) > 100 * 65536 * 4
+    assert L.nz_binomial_band_cap(130560, 80.0) > 2 * 12 * 181
+
+
+def test_dtypes_match_reference_layout():
+    from pypercolate_gb300 import hpc
+    assert np.dtype(hpc.microcanonical_statistics_dtype(True)).itemsize == 53
+    assert np.dtype(hpc.microcanonical_statistics_dtype(False)).itemsize == 52
+    assert np.dtype(hpc.canonical_statistics_dtype(True)).itemsize == 56
+    assert np.dtype(hpc.canonical_averages_dtype(True)).itemsize == 116
+    assert np.dtype(hpc.canonical_averages_dtype(False)).itemsize == 100
+    assert np.dtype(hpc.finalized_canonical_averages_dtype(True)).itemsize == 244
+    assert np.dtype(hpc.finalized_canonical_averages_dtype(False)).itemsize == 212
+    for sc in (True, False):
+        names = np.dtype(hpc.finalized_canonical_averages_dtype(sc)).names
+        assert ('percolation_probability_ci' in names) == sc
+    assert hpc.bond_finalize_canonical_averages is hpc.finalize_canonical_averages
+
+
+def test_seed_parsing_matches_numpy_rules():
+    from pypercolate_gb300 import hpc
+    w, n = hpc._mt_seed_words(42)
+    assert n == 0 and w[0] == 42
+    w, n = hpc._mt_seed_words([1, 2, 3])
+    assert n == 3 and list(w) == [1, 2, 3]
+    with pytest.raises(ValueError):
+        hpc._mt_seed_words(-1)
+    with pytest.raises(ValueError):
+        hpc._mt_seed_words(2 ** 32)
+    with pytest.raises(ValueError):
+        hpc._mt_seed_words([])
+
+
+def test_lattice_standin_matches_networkx():
+    nx = pytest.importorskip('networkx')
+    from pypercolate_gb300.percolate import LatticeGraph, percolation_graph
+    from pypercolate_gb300 import percolate as P
+    for L in (1, 2, 3, 5):
+        g = P.spanning_2d_grid(L)
+        pg = percolation_graph(g)
+        sg = LatticeGraph('grid', L)
+        assert list(pg['perc_graph'].edges()) == sg.edges()
+        assert list(pg['perc_graph'].nodes()) == sg.perc().nodes()
+        assert pg['num_edges'] == 2 * L * (L - 1)
+    for L in (1, 2, 7):
+        pg = percolation_graph(P.spanning_1d_chain(L))
+        assert list(pg['perc_graph'].edges()) == LatticeGraph('chain', L).edges()
+
+
+def test_graph_spec_side_masks():
+    nx = pytest.importorskip('networkx')
+    from pypercolate_gb300 import hpc
+    from pypercolate_gb300.percolate import percolation_graph
+    from conftest import load_golden
+    z = load_golden('kat_3x3.npz')
+    g = nx.Graph()
+    g.add_nodes_from(range(9))
+    g.add_edges_from([(i, i + j) for i in [1, 4, 7] for j in [-1, 1]])
+    g.add_edges_from([(i, i + j) for i in [3, 4, 5] for j in [-3, 3]])
+    g.add_nodes_from(range(9, 12), span=0)
+    g.add_nodes_from(range(12, 15), span=1)
+    g.add_edges_from([(0, 9), (3, 10), (6, 11)], span=0)
+    g.add_edges_from([(2, 12), (5, 13), (8, 14)], span=1)
+    pg = percolation_graph(g)
+    spec = hpc.graph_spec(**pg)
+    assert spec.kind == 2
+    assert np.array_equal(spec.eu, z['eu']) and np.array_equal(spec.ev, z['ev'])
+    assert np.array_equal(spec.side, z['side'])
+    # implicit lattice for the package's own builders
+    from pypercolate_gb300 import percolate as P
+    spec = hpc.graph_spec(**percolation_graph(P.spanning_2d_grid(8)))
+    assert spec.kind == 0 and spec.M == 112
+    # non-spanning on the same graph falls back to the explicit (L+2) x L grid
+    spec = hpc.graph_spec(**percolation_graph(P.spanning_2d_grid(4), spanning_cluster=False))
+    assert spec.kind == 2 and spec.N == 24

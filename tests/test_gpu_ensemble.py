@@ -1,0 +1,159 @@
+"""GPU ensemble path (batched runs, fused reductions, banded convolution)
+against the CPU oracle on the same Philox runs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from pypercolate_gb300 import _native as nat
+    nat.lib_handle()
+    return nat
+
+
+def _oracle_canonical(oracle, kind, L, key, run0, R, ps):
+    """Per-run canonical values with the same banded FP64 weights the GPU
+    computes, merged by the pairwise formula (exact oracle pipeline)."""
+    return oracle.ensemble_canonical(kind, L, key, run0, R, ps, n_threads=8)
+
+
+@pytest.mark.parametrize('kind,L', [(0, 8), (0, 24), (1, 500)])
+def test_ensemble_fp64_matches_oracle(gpu, oracle, kind, L):
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.0, 1.0, 41)
+    R = 300
+    ens = Ensemble('grid' if kind == 0 else 'chain', L, ps, precision='fp64', micro=False)
+    ens.run(R, key=77, run0=0)
+    ca = ens.canonical_averages()
+    mean, m2 = _oracle_canonical(oracle, kind, L, 77, 0, R, ps)
+    assert np.all(ca['number_of_runs'] == R)
+    np.testing.assert_allclose(ca['percolation_probability_mean'], mean[:, 0], rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(ca['max_cluster_size_mean'], mean[:, 1], rtol=1e-9)
+    np.testing.assert_allclose(ca['moments_mean'], mean[:, 2:], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(ca['max_cluster_size_m2'], m2[:, 1], rtol=1e-7, atol=1e-6)
+    np.testing.assert_allclose(ca['moments_m2'], m2[:, 2:], rtol=1e-7, atol=1e-6)
+
+
+def test_ensemble_fp32_error_budget(gpu, oracle):
+    """FP32 convolution: spanning probability and percolation strength within
+    1e-6 absolute of the FP64 pipeline; moments within 2e-6 relative."""
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.0, 1.0, 101)
+    L, R = 32, 256
+    ens = Ensemble('grid', L, ps, precision='fp32', micro=False)
+    ens.run(R, key=3, run0=0)
+    ca = ens.canonical_averages()
+    mean, _ = _oracle_canonical(oracle, 0, L, 3, 0, R, ps)
+    N = L * L
+    assert np.max(np.abs(ca['percolation_probability_mean'] - mean[:, 0])) < 1e-6
+    assert np.max(np.abs(ca['max_cluster_size_mean'] - mean[:, 1]) / N) < 1e-6
+    rel = np.abs(ca['moments_mean'] - mean[:, 2:]) / np.maximum(np.abs(mean[:, 2:]), 1e-30)
+    assert np.max(rel) < 2e-6
+
+
+def test_ensemble_accumulates_across_calls(gpu):
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.2, 0.8, 13)
+    a = Ensemble('grid', 12, ps, precision='fp64', micro=True)
+    a.run(100, key=1, run0=0).run(150, key=1, run0=100)
+    b = Ensemble('grid', 12, ps, precision='fp64', micro=True)
+    b.run(250, key=1, run0=0)
+    ca, cb = a.canonical_averages(), b.canonical_averages()
+    assert np.all(ca['number_of_runs'] == 250)
+    for k in ('percolation_probability_mean', 'max_cluster_size_mean', 'moments_mean'):
+        np.testing.assert_allclose(ca[k], cb[k], rtol=1e-12, atol=1e-14)
+    for k in ('max_cluster_size_m2', 'moments_m2'):
+        np.testing.assert_allclose(ca[k], cb[k], rtol=1e-9, atol=1e-9)
+    sa, sb = a.micro_sums(), b.micro_sums()
+    assert sa['count'] == sb['count'] == 250
+    assert np.array_equal(sa['span_count'], sb['span_count'])
+    assert (sa['sums'] == sb['sums']).all()
+    np.testing.assert_allclose(sa['m2'], sb['m2'], rtol=1e-9, atol=1e-6)
+
+
+@pytest.mark.parametrize('window', [0, 37])
+def test_fused_micro_reductions_exact(gpu, oracle, window):
+    """Exact per-n sums over runs of max and every moment (Python ints), the
+    spanning counts, and FP64 M2, against the oracle's exact integers."""
+    from pypercolate_gb300.ensemble import Ensemble
+    L, R = 10, 97
+    ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True, window=window)
+    ens.run(R, key=11, run0=5)
+    got = ens.micro_sums()
+    M = 2 * L * (L - 1)
+    N = L * L
+    vals = np.zeros((6, R, M + 1), dtype=object)
+    span = np.zeros(M + 1, dtype=np.int64)
+    for r in range(R):
+        run = oracle.lattice_run(0, L, oracle.philox_permutation(11, 5 + r, M))
+        lo = run['moments_u64'].astype(object)
+        hi = run['moments_hi'].astype(object)
+        exact = lo + hi * (1 << 64)
+        vals[0, r] = run['max'].astype(object)
+        vals[1, r] = exact[:, 0]
+        vals[2, r] = N - run['max'].astype(object)
+        vals[3, r] = exact[:, 2]
+        vals[4, r] = exact[:, 3]
+        vals[5, r] = exact[:, 4]
+        span += run['span']
+    assert got['count'] == R
+    assert np.array_equal(got['span_count'], span.astype(np.uint64))
+    assert (got['sums'] == vals.sum(axis=1)).all()
+    fl = vals.astype(np.float64)
+    m2 = ((fl - fl.mean(axis=1, keepdims=True)) ** 2).sum(axis=1)
+    np.testing.assert_allclose(got['m2'], m2, rtol=1e-9, atol=1e-6)
+
+
+def test_microcanonical_averages_semantics(gpu, oracle):
+    """Classic microcanonical averages (percolate/percolate.py:450-705)."""
+    from pypercolate_gb300.ensemble import Ensemble
+    L, R, alpha = 6, 60, 0.3173
+    ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True)
+    ens.run(R, key=2, run0=0)
+    got = ens.microcanonical_averages(alpha)
+    M, N = 2 * L * (L - 1), L * L
+    mx, sp, mom = [], [], []
+    for r in range(R):
+        run = oracle.lattice_run(0, L, oracle.philox_permutation(2, r, M))
+        mx.append(run['max'].astype(np.float64))
+        sp.append(run['span'])
+        mom.append(run['moments_f64'])
+    mx, sp, mom = np.array(mx), np.array(sp), np.array(mom)
+    mean, lo, hi = oracle.microcanonical_average_spanning(sp.sum(0), R, alpha)
+    np.testing.assert_allclose(got['spanning_cluster'], mean, rtol=1e-12)
+    np.testing.assert_allclose(got['spanning_cluster_ci'][:, 0], lo, rtol=1e-8, atol=1e-14)
+    np.testing.assert_allclose(got['spanning_cluster_ci'][:, 1], hi, rtol=1e-8)
+    mlo, mhi = oracle.microcanonical_average_normal(mx.mean(0), mx.std(0, ddof=1), R, alpha)
+    np.testing.assert_allclose(got['max_cluster_size'], mx.mean(0) / N, rtol=1e-12)
+    np.testing.assert_allclose(got['max_cluster_size_ci'][:, 0], mlo / N, rtol=1e-9)
+    np.testing.assert_allclose(got['max_cluster_size_ci'][:, 1], mhi / N, rtol=1e-9)
+    for k in range(5):
+        np.testing.assert_allclose(got['moments'][k], mom[:, :, k].mean(0) / N, rtol=1e-12)
+        klo, khi = oracle.microcanonical_average_normal(mom[:, :, k].mean(0),
+                                                        mom[:, :, k].std(0, ddof=1), R, alpha)
+        np.testing.assert_allclose(got['moments_ci'][k][:, 0], klo / N, rtol=1e-8, atol=1e-12)
+
+
+def test_finalized_ensemble(gpu):
+    """Ensemble.finalized() == finalize_canonical_averages(canonical_averages())."""
+    from pypercolate_gb300.ensemble import Ensemble
+    from pypercolate_gb300 import hpc
+    import scipy.stats
+    ps = np.linspace(0.3, 0.7, 9)
+    ens = Ensemble('grid', 16, ps, precision='fp64', micro=False)
+    ens.run(200, key=9)
+    fin = ens.finalized(0.05)
+    ca = ens.canonical_averages()
+    n = ca['number_of_runs'].astype(np.float64)
+    std = np.sqrt(ca['max_cluster_size_m2'] / (n - 1)) / 256
+    np.testing.assert_allclose(fin['percolation_strength_std'], std, rtol=1e-12)
+    lo, hi = scipy.stats.t.interval(0.95, df=n - 1, loc=fin['percolation_strength_mean'],
+                                    scale=std / np.sqrt(n))
+    np.testing.assert_allclose(fin['percolation_strength_ci'][:, 0], lo, rtol=1e-10)
+    np.testing.assert_allclose(fin['percolation_strength_ci'][:, 1], hi, rtol=1e-10)
+    assert np.all(fin['p'] == ps)

@@ -223,34 +223,63 @@ void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, co
 // =====================================================================
 // Banded convolution of record windows (ensemble path)
 // =====================================================================
-// Statistic s of run r at row n (record planes of the window).
-__device__ __forceinline__ double record_value(const NzRecords &rec, size_t off, int s, uint32_t N) {
-    switch (s) {
-        case 0: return (rec.max_span[off] & kSpanBit) ? 1.0 : 0.0;
-        case 1: return (double)(rec.max_span[off] & ~kSpanBit);
-        case 2: return (double)rec.m0[off];
-        case 3: return (double)(N - (rec.max_span[off] & ~kSpanBit));
-        case 4: return (double)rec.m2[off];
-        case 5: return (double)rec.m3[off];
-        default: return ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off];
-    }
+// Statistic S of the record at `off` (S = 0 spanning, 1 max, 2 m0, 3 m1,
+// 4 m2, 5 m3, 6 m4).  The FP32 loader splits 64-bit words into 32-bit halves
+// so that every conversion stays on the FP32 pipe.
+template <int S>
+__device__ __forceinline__ double record_value(const NzRecords &rec, size_t off, uint32_t N) {
+    if (S == 0) return (rec.max_span[off] & kSpanBit) ? 1.0 : 0.0;
+    if (S == 1) return (double)(rec.max_span[off] & ~kSpanBit);
+    if (S == 2) return (double)rec.m0[off];
+    if (S == 3) return (double)(N - (rec.max_span[off] & ~kSpanBit));
+    if (S == 4) return (double)rec.m2[off];
+    if (S == 5) return (double)rec.m3[off];
+    return ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off];
 }
 
-__device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off, int s, uint32_t N) {
-    switch (s) {
-        case 0: return (rec.max_span[off] & kSpanBit) ? 1.0f : 0.0f;
-        case 1: return (float)(rec.max_span[off] & ~kSpanBit);
-        case 2: return (float)rec.m0[off];
-        case 3: return (float)(N - (rec.max_span[off] & ~kSpanBit));
-        case 4: return __ull2float_rn(rec.m2[off]);
-        case 5: return __ull2float_rn(rec.m3[off]);
-        default: return (float)(ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off]);
-    }
+__device__ __forceinline__ float u64_to_f32(uint64_t x) {
+    return fmaf((float)(uint32_t)(x >> 32), 4294967296.0f, (float)(uint32_t)x);
+}
+
+template <int S>
+__device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off, uint32_t N) {
+    if (S == 0) return (rec.max_span[off] & kSpanBit) ? 1.0f : 0.0f;
+    if (S == 1) return (float)(rec.max_span[off] & ~kSpanBit);
+    if (S == 2) return (float)rec.m0[off];
+    if (S == 3) return (float)(N - (rec.max_span[off] & ~kSpanBit));
+    if (S == 4) return u64_to_f32(rec.m2[off]);
+    if (S == 5) return u64_to_f32(rec.m3[off]);
+    return fmaf((float)rec.m4_hi[off], 18446744073709551616.0f, u64_to_f32(rec.m4_lo[off]));
 }
 
 constexpr int kConvRuns = 128;  // runs per CTA (one per thread)
 constexpr int kConvPT = 16;     // probabilities per CTA
 constexpr int kConvChunk = 64;  // rows staged per step
+
+// grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
+// kConvPT canonical values of its run for one statistic over the window's
+// rows, with the tile's weights staged in shared memory (zero outside each
+// p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
+// products summed in FP32 over kConvChunk rows, then added into FP64.
+template <int PRECISION, int S>
+__device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
+                                          const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
+                                          double *acc) {
+    using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
+    wtype part[kConvPT];
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) part[j] = 0;
+    const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
+    for (uint32_t i = 0; i < cn; ++i) {
+        const size_t off = base + (size_t)i * p.rec.run_stride;
+        const wtype q = PRECISION == 0 ? (wtype)record_value<S>(p.rec, off, p.N)
+                                       : (wtype)record_value_f<S>(p.rec, off, p.N);
+#pragma unroll
+        for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
+}
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
 // kConvPT canonical values of its run for one statistic over the window's
@@ -302,18 +331,15 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
         }
         __syncthreads();
         if (r < p.n_runs) {
-            wtype part[kConvPT];
-#pragma unroll
-            for (int j = 0; j < kConvPT; ++j) part[j] = 0;
-            for (uint32_t i = 0; i < cn; ++i) {
-                const size_t off = (size_t)(c0 + i - p.n_begin) * p.rec.run_stride + r;
-                const wtype q = PRECISION == 0 ? (wtype)record_value(p.rec, off, s, p.N)
-                                               : (wtype)record_value_f(p.rec, off, s, p.N);
-#pragma unroll
-                for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
+            switch (s) {
+                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, acc); break;
+                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, acc); break;
+                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, acc); break;
+                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, acc); break;
+                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, acc); break;
+                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, acc); break;
+                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, acc); break;
             }
-#pragma unroll
-            for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
         }
     }
     if (r < p.n_runs) {
@@ -411,96 +437,156 @@ void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t
 // =====================================================================
 // Per (row n, statistic): exact integer sum over runs and the sum of squared
 // deviations, merged into the accumulators with the pairwise formula.
-// Statistics: 0 max, 1 m0, 2 m1 (= N - max), 3 m2, 4 m3, 5 m4; plus the
-// count of spanning runs.  Squares are taken of the deviation from run 0's
-// value (an exact 128-bit integer, converted to FP64), which keeps the FP64
-// sum free of cancellation.
-__device__ __forceinline__ void record_u128(const NzRecords &rec, size_t off, int s, uint32_t N, uint64_t &lo,
-                                            uint64_t &hi) {
-    hi = 0;
-    switch (s) {
-        case 0: lo = rec.max_span[off] & ~kSpanBit; break;
-        case 1: lo = rec.m0[off]; break;
-        case 2: lo = N - (rec.max_span[off] & ~kSpanBit); break;
-        case 3: lo = rec.m2[off]; break;
-        case 4: lo = rec.m3[off]; break;
-        default: lo = rec.m4_lo[off]; hi = rec.m4_hi[off]; break;
+// Statistics: 0 max, 1 m0, 2 m1 (= N - max), 3 m2, 4 m3, 5 m4; block 6
+// counts the spanning runs.  Deviations are taken from run 0's value x0:
+//   max, m0, m1 (< 2^21) and m2 (< 2^42): d = x - x0 as int64, d^2 summed
+//     exactly (u64 / u128), and M2 = (R * sum d^2 - (sum d)^2) / R from the
+//     exact 128-bit numerator;
+//   m3, m4: d exact as a 128-bit integer, squared and summed in FP64 (the
+//     shift keeps the FP64 sum free of cancellation).
+typedef unsigned __int128 u128;
+typedef __int128 i128;
+
+__device__ __forceinline__ u128 shfl_down_u128(u128 v, int off) {
+    uint64_t lo = (uint64_t)v, hi = (uint64_t)(v >> 64);
+    lo = __shfl_down_sync(0xffffffffu, lo, off);
+    hi = __shfl_down_sync(0xffffffffu, hi, off);
+    return ((u128)hi << 64) | lo;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ u128 block_sum_u128(u128 v, u128 *s_tmp) {
+    for (int off = 16; off > 0; off >>= 1) v += shfl_down_u128(v, off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) s_tmp[warp] = v;
+    __syncthreads();
+    u128 t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < BLOCK / 32; ++w) t += s_tmp[w];
+    return t;  // valid in thread 0
+}
+
+template <int BLOCK>
+__device__ __forceinline__ double block_sum_f64(double v, double *s_tmp) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) s_tmp[warp] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < BLOCK / 32; ++w) t += s_tmp[w];
+    return t;
+}
+
+__device__ __forceinline__ double u128_to_f64(u128 x) {
+    return ldexp((double)(uint64_t)(x >> 64), 64) + (double)(uint64_t)x;
+}
+
+__device__ __forceinline__ double i128_to_f64(i128 x) {
+    return x < 0 ? -u128_to_f64((u128)(-x)) : u128_to_f64((u128)x);
+}
+
+template <int S>
+__device__ __forceinline__ u128 micro_value(const NzRecords &rec, size_t off, uint32_t N) {
+    if (S == 0) return rec.max_span[off] & ~kSpanBit;
+    if (S == 1) return rec.m0[off];
+    if (S == 2) return N - (rec.max_span[off] & ~kSpanBit);
+    if (S == 3) return rec.m2[off];
+    if (S == 4) return rec.m3[off];
+    return ((u128)rec.m4_hi[off] << 64) | rec.m4_lo[off];
+}
+
+template <int BLOCK, int S>
+__device__ void micro_stat(const MicroParams &p, uint32_t n, size_t row, u128 *s_u, double *s_f) {
+    const u128 x0 = micro_value<S>(p.rec, row, p.N);
+    u128 sx = 0;        // exact sum of x
+    i128 sd = 0;        // exact sum of d = x - x0
+    u128 sq = 0;        // exact sum of d^2 (S <= 3)
+    double fsq = 0.0;   // FP64 sum of d^2 (S >= 4)
+    for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
+        const u128 x = micro_value<S>(p.rec, row + r, p.N);
+        sx += x;
+        if (S <= 2) {
+            const int64_t d = (int64_t)(uint64_t)x - (int64_t)(uint64_t)x0;
+            sd += d;
+            sq += (uint64_t)(d * d);
+        } else if (S == 3) {
+            const int64_t d = (int64_t)(uint64_t)x - (int64_t)(uint64_t)x0;
+            sd += d;
+            const uint64_t ad = (uint64_t)(d < 0 ? -d : d);
+            sq += (u128)ad * ad;
+        } else {
+            const i128 d = (i128)x - (i128)x0;
+            sd += d;
+            const double fd = i128_to_f64(d);
+            fsq = fma(fd, fd, fsq);
+        }
+    }
+    const u128 tx = block_sum_u128<BLOCK>(sx, s_u);
+    const u128 tsd_u = block_sum_u128<BLOCK>((u128)sd, s_u);  // two's complement sum
+    const i128 tsd = (i128)tsd_u;
+    double m2b;
+    if (S <= 3) {
+        const u128 tq = block_sum_u128<BLOCK>(sq, s_u);
+        if (threadIdx.x == 0) {
+            const u128 ad = (u128)(tsd < 0 ? -tsd : tsd);
+            if ((tq >> 103) == 0 && (ad >> 63) == 0) {
+                // R * sum d^2 - (sum d)^2 >= 0, exact in 128 bits (R < 2^25)
+                const u128 num = (u128)(uint64_t)p.n_runs * tq - ad * ad;
+                m2b = u128_to_f64(num) / (double)p.n_runs;
+            } else {
+                const double fsd = u128_to_f64(ad);
+                m2b = u128_to_f64(tq) - fsd * fsd / (double)p.n_runs;
+                if (m2b < 0.0) m2b = 0.0;
+            }
+        }
+    } else {
+        const double tf = block_sum_f64<BLOCK>(fsq, s_f);
+        if (threadIdx.x == 0) {
+            const double fsd = i128_to_f64(tsd);
+            m2b = tf - fsd * fsd / (double)p.n_runs;
+            if (m2b < 0.0) m2b = 0.0;
+        }
+    }
+    if (threadIdx.x == 0) {
+        const double R = (double)p.n_runs;
+        const double mean_b = u128_to_f64(tx) / R;
+        const size_t idx = (size_t)S * (p.M + 1) + n;
+        const double na = (double)*p.count_before;
+        const u128 a = ((u128)p.acc.sum_hi[idx] << 64) | p.acc.sum_lo[idx];
+        const double mean_a = na > 0 ? u128_to_f64(a) / na : 0.0;
+        double nn = na, mm = mean_a, ss = p.acc.m2[idx];
+        chan_merge(nn, mm, ss, R, mean_b, m2b);
+        const u128 t = a + tx;
+        p.acc.sum_lo[idx] = (uint64_t)t;
+        p.acc.sum_hi[idx] = (uint64_t)(t >> 64);
+        p.acc.m2[idx] = ss;
     }
 }
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
     const uint32_t n = p.n_begin + blockIdx.x;
-    const int s = blockIdx.y;  // 0..5 statistics, 6 = spanning count
+    const int s = blockIdx.y;
     const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;
-    __shared__ uint64_t s_lo[BLOCK], s_hi[BLOCK], s_cnt[BLOCK];
-    __shared__ double s_sq[BLOCK];
-    __shared__ double s_d[BLOCK];
+    __shared__ u128 s_u[BLOCK / 32];
+    __shared__ double s_f[BLOCK / 32];
     if (s == 6) {
-        uint64_t c = 0;
-        for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) c += (p.rec.max_span[row + r] & kSpanBit) ? 1u : 0u;
-        s_cnt[threadIdx.x] = c;
-        __syncthreads();
-        for (int off = BLOCK / 2; off > 0; off >>= 1) {
-            if (threadIdx.x < (unsigned)off) s_cnt[threadIdx.x] += s_cnt[threadIdx.x + off];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) p.acc.span_count[n] += s_cnt[0];
+        uint32_t c = 0;
+        for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) c += (p.rec.max_span[row + r] >> 31);
+        const u128 t = block_sum_u128<BLOCK>(c, s_u);
+        if (threadIdx.x == 0) p.acc.span_count[n] += (uint64_t)t;
         return;
     }
-    uint64_t x0lo, x0hi;
-    record_u128(p.rec, row, s, p.N, x0lo, x0hi);
-    uint64_t slo = 0, shi = 0;  // exact sum (unsigned 128)
-    double sd = 0.0, sq = 0.0;  // sum of deviations and squared deviations
-    for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
-        uint64_t lo, hi;
-        record_u128(p.rec, row + r, s, p.N, lo, hi);
-        uint64_t nlo = slo + lo;
-        shi += hi + (nlo < slo ? 1ull : 0ull);
-        slo = nlo;
-        // deviation from run 0 as a signed 128-bit value -> double
-        uint64_t dlo = lo - x0lo;
-        uint64_t dhi = hi - x0hi - (lo < x0lo ? 1ull : 0ull);
-        double d;
-        if ((int64_t)dhi < 0) {  // negative: negate
-            uint64_t nlo2 = ~dlo + 1ull;
-            uint64_t nhi2 = ~dhi + (nlo2 == 0 ? 1ull : 0ull);
-            d = -(ldexp((double)nhi2, 64) + (double)nlo2);
-        } else {
-            d = ldexp((double)dhi, 64) + (double)dlo;
-        }
-        sd += d;
-        sq = fma(d, d, sq);
-    }
-    s_lo[threadIdx.x] = slo; s_hi[threadIdx.x] = shi; s_sq[threadIdx.x] = sq; s_d[threadIdx.x] = sd;
-    __syncthreads();
-    for (int off = BLOCK / 2; off > 0; off >>= 1) {
-        if (threadIdx.x < (unsigned)off) {
-            uint64_t a = s_lo[threadIdx.x], b = s_lo[threadIdx.x + off];
-            uint64_t nlo = a + b;
-            s_hi[threadIdx.x] += s_hi[threadIdx.x + off] + (nlo < a ? 1ull : 0ull);
-            s_lo[threadIdx.x] = nlo;
-            s_sq[threadIdx.x] += s_sq[threadIdx.x + off];
-            s_d[threadIdx.x] += s_d[threadIdx.x + off];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double R = (double)p.n_runs;
-        const double sumd = s_d[0];
-        double m2b = s_sq[0] - sumd * sumd / R;
-        if (m2b < 0.0) m2b = 0.0;
-        const double mean_b = (ldexp((double)s_hi[0], 64) + (double)s_lo[0]) / R;
-        const size_t idx = (size_t)s * (p.M + 1) + n;
-        const double na = (double)*p.count_before;
-        const uint64_t alo = p.acc.sum_lo[idx], ahi = p.acc.sum_hi[idx];
-        const double mean_a = na > 0 ? (ldexp((double)ahi, 64) + (double)alo) / na : 0.0;
-        double nn = na, mm = mean_a, ss = p.acc.m2[idx];
-        chan_merge(nn, mm, ss, R, mean_b, m2b);
-        uint64_t nlo = alo + s_lo[0];
-        p.acc.sum_hi[idx] = ahi + s_hi[0] + (nlo < alo ? 1ull : 0ull);
-        p.acc.sum_lo[idx] = nlo;
-        p.acc.m2[idx] = ss;
+    switch (s) {
+        case 0: micro_stat<BLOCK, 0>(p, n, row, s_u, s_f); break;
+        case 1: micro_stat<BLOCK, 1>(p, n, row, s_u, s_f); break;
+        case 2: micro_stat<BLOCK, 2>(p, n, row, s_u, s_f); break;
+        case 3: micro_stat<BLOCK, 3>(p, n, row, s_u, s_f); break;
+        case 4: micro_stat<BLOCK, 4>(p, n, row, s_u, s_f); break;
+        default: micro_stat<BLOCK, 5>(p, n, row, s_u, s_f); break;
     }
 }
 

@@ -151,18 +151,22 @@ def test_exact_records_vs_oracle(gpu, oracle, kind, L, R):
         assert np.array_equal(h['edge'][1:, r], ref['edge'][1:])
 
 
-def test_exact_beyond_uint64_L512(gpu, oracle):
-    """At L=512 sum s^4 exceeds 2**64: the high word is exact."""
+def test_exact_beyond_uint64_L724(gpu, oracle):
+    """At L=724 sum' s^4 exceeds 2**64 in these runs: the high word is exact."""
     from pypercolate_gb300 import hpc
-    spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, 512)
-    rec = hpc._run_microcanonical(spec, True, rng='philox', key=5, run0=0, n_runs=2,
+    spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, 724)
+    rec = hpc._run_microcanonical(spec, True, rng='philox', key=5, run0=0, n_runs=3,
                                   with_edge=False)
     h = rec.host()
-    for r in range(2):
-        ref = oracle.lattice_run(0, 512, oracle.philox_permutation(5, r, spec.M))
-        assert ref['moments_hi'][:, 4].max() > 0
+    wrapped = 0
+    for r in range(3):
+        ref = oracle.lattice_run(0, 724, oracle.philox_permutation(5, r, spec.M))
+        wrapped += int(ref['moments_hi'][:, 4].max() > 0)
         assert np.array_equal(h['m4_hi'][:, r].astype(np.uint64), ref['moments_hi'][:, 4])
         assert np.array_equal(h['m4_lo'][:, r], ref['moments_u64'][:, 4])
+        assert np.array_equal(h['m3'][:, r], ref['moments_u64'][:, 3])
+        assert np.array_equal(h['max_span'][:, r] & 0x7fffffff, ref['max'])
+    assert wrapped == 3
 
 
 def test_edge_cases(gpu):

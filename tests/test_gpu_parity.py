@@ -252,8 +252,8 @@ def test_student_t_quantile(gpu):
     q, d = np.meshgrid(qs, dfs)
     q, d = q.ravel(), d.ravel()
     out = torch.empty(q.size, dtype=torch.float64, device='cuda')
-    gpu.check(gpu.lib_handle().nz_student_t_quantile(
-        gpu.ptr(torch.from_numpy(q).cuda()), gpu.ptr(torch.from_numpy(d).cuda()), q.size,
-        gpu.ptr(out), gpu.stream_handle()), 'tq')
+    d_q, d_d = torch.from_numpy(q.copy()).cuda(), torch.from_numpy(d.copy()).cuda()
+    gpu.check(gpu.lib_handle().nz_student_t_quantile(gpu.ptr(d_q), gpu.ptr(d_d), q.size,
+                                                     gpu.ptr(out), gpu.stream_handle()), 'tq')
     np.testing.assert_allclose(out.cpu().numpy(), scipy.stats.t.ppf(q, d), rtol=1e-10,
                                atol=1e-12)

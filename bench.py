@@ -48,6 +48,8 @@ def parse():
     ap.add_argument('--window', type=int, default=0)
     ap.add_argument('--cpu-sample', type=int, default=256, help='runs in the CPU baseline sample')
     ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--l2-fetch', type=int, default=32,
+                    help='L2 fetch granularity of this process (bytes; 0 = leave as is)')
     return ap.parse_args()
 
 
@@ -189,6 +191,9 @@ def main():
     from pypercolate_gb300.ensemble import Ensemble
 
     L, R = args.L, args.runs
+    if args.l2_fetch:
+        nat.set_l2_fetch_granularity(args.l2_fetch)
+    l2_fetch = nat.get_l2_fetch_granularity()
     ps = np.linspace(0.0, 1.0, args.P)
     N, M = L * L, 2 * L * (L - 1)
     ens = Ensemble('grid', L, ps, precision=args.precision, micro=not args.no_micro,
@@ -268,7 +273,7 @@ def main():
                                '%d uniform p in [0,1], fused micro reductions=%s'
                                % (L, R, args.P, not args.no_micro),
                    'L': L, 'N': N, 'M': M, 'runs_per_step': R, 'P': args.P,
-                   'precision': args.precision,
+                   'precision': args.precision, 'l2_fetch_bytes': l2_fetch,
                    'l2': 'inputs larger than L2 (%.1f GB of union-find state per step)'
                          % (R * N * 4 / 1e9)},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',

@@ -216,6 +216,16 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
                 double *acc_mean, double *acc_m2, const NzMicroAccum *micro,
                 void *stream);
 
+/* ---- memory-system hint ------------------------------------------------ */
+/* L2 fetch granularity of the calling CUDA context (cudaLimitMaxL2FetchGranularity:
+ * 0, 32, 64 or 128 bytes).  The union-find reads scattered 4-byte node words;
+ * 32-byte fetches avoid pulling a second, unused sector from HBM per miss.
+ * The limit belongs to the caller's context (it ends with the process) and
+ * applies to every kernel of that context, so the library never sets it on
+ * its own.  (No counterpart in the reference.) */
+int nz_set_l2_fetch_granularity(int32_t bytes);
+int nz_get_l2_fetch_granularity(int32_t *bytes);
+
 /* ---- measurement ------------------------------------------------------ */
 /* When enabled, every launch sequence of a category below is bracketed by
  * CUDA events recorded on the caller's stream.  nz_profile_read waits for

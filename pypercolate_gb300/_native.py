@@ -92,6 +92,8 @@ _SIGNATURES = [
      [ctypes.POINTER(NzMicroAccum), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
       ctypes.c_double, _vp, _vp]),
     ('nz_student_t_quantile', ctypes.c_int, [_vp, _vp, ctypes.c_int32, _vp, _vp]),
+    ('nz_set_l2_fetch_granularity', ctypes.c_int, [ctypes.c_int32]),
+    ('nz_get_l2_fetch_granularity', ctypes.c_int, [_vp]),
     ('nz_profile_enable', None, [ctypes.c_int32]),
     ('nz_profile_read', ctypes.c_int, [ctypes.c_int32, _vp, _vp]),
     ('nz_ensemble_workspace_bytes', ctypes.c_size_t,
@@ -135,6 +137,19 @@ def lib_handle(build_if_missing=True):
                 fn.argtypes = args
             _lib = lib
     return _lib
+
+
+def set_l2_fetch_granularity(nbytes):
+    """Context-wide L2 fetch granularity hint (0, 32, 64, 128 bytes)."""
+    torch_cuda()
+    check(lib_handle().nz_set_l2_fetch_granularity(int(nbytes)), 'nz_set_l2_fetch_granularity')
+
+
+def get_l2_fetch_granularity():
+    torch_cuda()
+    v = ctypes.c_int32()
+    check(lib_handle().nz_get_l2_fetch_granularity(ctypes.byref(v)), 'nz_get_l2_fetch_granularity')
+    return v.value
 
 
 PROF_CATEGORIES = ('setup', 'union_find', 'micro', 'conv', 'reduce')

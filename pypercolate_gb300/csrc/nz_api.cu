@@ -167,6 +167,19 @@ int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs, in
     return check_launch();
 }
 
+int nz_set_l2_fetch_granularity(int32_t bytes) {
+    if (bytes != 0 && bytes != 32 && bytes != 64 && bytes != 128) return NZ_ERR_INVALID;
+    return cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes) == cudaSuccess ? NZ_OK : NZ_ERR_CUDA;
+}
+
+int nz_get_l2_fetch_granularity(int32_t *bytes) {
+    if (!bytes) return NZ_ERR_INVALID;
+    size_t v = 0;
+    if (cudaDeviceGetLimit(&v, cudaLimitMaxL2FetchGranularity) != cudaSuccess) return NZ_ERR_CUDA;
+    *bytes = (int32_t)v;
+    return NZ_OK;
+}
+
 void nz_profile_enable(int32_t enabled) {
     std::lock_guard<std::mutex> lk(g_prof.mu);
     g_prof.enabled = enabled != 0;

@@ -234,7 +234,7 @@ __device__ __forceinline__ double record_value(const NzRecords &rec, size_t off,
     if (S == 3) return (double)(N - (rec.max_span[off] & ~kSpanBit));
     if (S == 4) return (double)rec.m2[off];
     if (S == 5) return (double)rec.m3[off];
-    return ldexp((double)rec.m4_hi[off], 64) + (double)rec.m4_lo[off];
+    return fma((double)rec.m4_hi[off], 18446744073709551616.0, (double)rec.m4_lo[off]);
 }
 
 __device__ __forceinline__ float u64_to_f32(uint64_t x) {
@@ -255,6 +255,7 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
 constexpr int kConvRuns = 128;  // runs per CTA (one per thread)
 constexpr int kConvPT = 16;     // probabilities per CTA
 constexpr int kConvChunk = 64;  // rows staged per step
+constexpr int kConvFlush = 8;   // chunks summed in FP32 before an FP64 flush
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
 // kConvPT canonical values of its run for one statistic over the window's
@@ -264,7 +265,7 @@ constexpr int kConvChunk = 64;  // rows staged per step
 template <int PRECISION, int S>
 __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                           const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
-                                          double *acc) {
+                                          typename std::conditional<PRECISION == 0, double, float>::type *mid) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     wtype part[kConvPT];
 #pragma unroll
@@ -278,7 +279,7 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
         for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
     }
 #pragma unroll
-    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
+    for (int j = 0; j < kConvPT; ++j) mid[j] += part[j];
 }
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
@@ -313,9 +314,13 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = s_range[0], nhi = s_range[1];
     if (nlo >= nhi) return;
+    // sums: FP32 over kConvChunk rows (part), FP32 over kConvFlush chunks
+    // (mid), FP64 beyond (acc); FP64 is a small fraction of the issue slots
     double acc[kConvPT];
+    wtype mid[kConvPT];
 #pragma unroll
-    for (int j = 0; j < kConvPT; ++j) acc[j] = 0.0;
+    for (int j = 0; j < kConvPT; ++j) { acc[j] = 0.0; mid[j] = 0; }
+    int chunk = 0;
     for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
         const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
         __syncthreads();
@@ -332,16 +337,23 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
         __syncthreads();
         if (r < p.n_runs) {
             switch (s) {
-                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, acc); break;
-                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, acc); break;
-                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, acc); break;
-                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, acc); break;
-                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, acc); break;
-                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, acc); break;
-                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, acc); break;
+                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, mid); break;
+                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, mid); break;
+                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, mid); break;
+                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, mid); break;
+                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, mid); break;
+                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, mid); break;
+                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, mid); break;
+            }
+            if (++chunk == kConvFlush) {
+                chunk = 0;
+#pragma unroll
+                for (int j = 0; j < kConvPT; ++j) { acc[j] += (double)mid[j]; mid[j] = 0; }
             }
         }
     }
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)mid[j];
     if (r < p.n_runs) {
 #pragma unroll
         for (int j = 0; j < kConvPT; ++j) {
@@ -481,119 +493,153 @@ __device__ __forceinline__ double block_sum_f64(double v, double *s_tmp) {
 }
 
 __device__ __forceinline__ double u128_to_f64(u128 x) {
-    return ldexp((double)(uint64_t)(x >> 64), 64) + (double)(uint64_t)x;
+    return fma((double)(uint64_t)(x >> 64), 18446744073709551616.0, (double)(uint64_t)x);
 }
 
 __device__ __forceinline__ double i128_to_f64(i128 x) {
     return x < 0 ? -u128_to_f64((u128)(-x)) : u128_to_f64((u128)x);
 }
 
-template <int S>
-__device__ __forceinline__ u128 micro_value(const NzRecords &rec, size_t off, uint32_t N) {
-    if (S == 0) return rec.max_span[off] & ~kSpanBit;
-    if (S == 1) return rec.m0[off];
-    if (S == 2) return N - (rec.max_span[off] & ~kSpanBit);
-    if (S == 3) return rec.m2[off];
-    if (S == 4) return rec.m3[off];
-    return ((u128)rec.m4_hi[off] << 64) | rec.m4_lo[off];
+constexpr double kTwo64 = 18446744073709551616.0;
+constexpr double kTwo32 = 4294967296.0;
+
+// Per-thread partial sums of one row: for every statistic the exact sum of
+// x, the exact sum of d = x - x0 and the sum of d^2 (exact integers for
+// max, m0, m2; FP64 for m3, m4), plus the spanning count.
+struct MicroPart {
+    uint64_t sx_max, sx_m0, sx_m2;  // max, m0 < 2^21; m2 < 2^42 (per-thread sums fit)
+    u128 sx_m3, sx_m4;
+    int64_t sd_max, sd_m0, sd_m2;
+    i128 sd_m3, sd_m4;
+    uint64_t sq_max, sq_m0;
+    u128 sq_m2;
+    double fq_m3, fq_m4;
+    uint32_t span;
+};
+
+__device__ __forceinline__ double i128_to_f64_fast(i128 d) {
+    // |d| < 2^95: hi part exact in FP64, one rounding in the final FMA
+    const int64_t hi = (int64_t)(d >> 32);
+    const uint32_t lo = (uint32_t)(uint64_t)d;
+    return fma((double)hi, kTwo32, (double)lo);
 }
 
-template <int BLOCK, int S>
-__device__ void micro_stat(const MicroParams &p, uint32_t n, size_t row, u128 *s_u, double *s_f) {
-    const u128 x0 = micro_value<S>(p.rec, row, p.N);
-    u128 sx = 0;        // exact sum of x
-    i128 sd = 0;        // exact sum of d = x - x0
-    u128 sq = 0;        // exact sum of d^2 (S <= 3)
-    double fsq = 0.0;   // FP64 sum of d^2 (S >= 4)
+template <int BLOCK>
+__device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_tmp[threadIdx.x >> 5] = v;
+    __syncthreads();
+    uint64_t t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < BLOCK / 32; ++w) t += s_tmp[w];
+    return t;
+}
+
+// One block per row n: reduces all statistics of that row over the runs and
+// merges them into the accumulators (pairwise formula for M2).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
+    const uint32_t n = p.n_begin + blockIdx.x;
+    const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;
+    const NzRecords &rec = p.rec;
+    __shared__ u128 s_u[BLOCK / 32];
+    __shared__ double s_f[BLOCK / 32];
+    __shared__ uint64_t s_w[BLOCK / 32];
+    const uint32_t x0_max = rec.max_span[row] & ~kSpanBit;
+    const uint32_t x0_m0 = rec.m0[row];
+    const uint64_t x0_m2 = rec.m2[row], x0_m3 = rec.m3[row];
+    const u128 x0_m4 = ((u128)rec.m4_hi[row] << 64) | rec.m4_lo[row];
+    MicroPart a = {};
     for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
-        const u128 x = micro_value<S>(p.rec, row + r, p.N);
-        sx += x;
-        if (S <= 2) {
-            const int64_t d = (int64_t)(uint64_t)x - (int64_t)(uint64_t)x0;
-            sd += d;
-            sq += (uint64_t)(d * d);
-        } else if (S == 3) {
-            const int64_t d = (int64_t)(uint64_t)x - (int64_t)(uint64_t)x0;
-            sd += d;
-            const uint64_t ad = (uint64_t)(d < 0 ? -d : d);
-            sq += (u128)ad * ad;
-        } else {
-            const i128 d = (i128)x - (i128)x0;
-            sd += d;
-            const double fd = i128_to_f64(d);
-            fsq = fma(fd, fd, fsq);
-        }
+        const size_t off = row + r;
+        const uint32_t ms = rec.max_span[off];
+        const uint32_t mx = ms & ~kSpanBit;
+        const uint32_t m0 = rec.m0[off];
+        const uint64_t m2 = rec.m2[off], m3 = rec.m3[off];
+        const u128 m4 = ((u128)rec.m4_hi[off] << 64) | rec.m4_lo[off];
+        a.span += ms >> 31;
+        a.sx_max += mx;
+        a.sx_m0 += m0;
+        a.sx_m2 += m2;
+        a.sx_m3 += m3;
+        a.sx_m4 += m4;
+        const int64_t dmax = (int64_t)mx - (int64_t)x0_max;
+        const int64_t dm0 = (int64_t)m0 - (int64_t)x0_m0;
+        const int64_t dm2 = (int64_t)m2 - (int64_t)x0_m2;
+        const int64_t dm3 = (int64_t)(m3 - x0_m3);  // |m3 - x0| < 2^63
+        const i128 dm4 = (i128)(m4 - x0_m4);
+        a.sd_max += dmax;
+        a.sd_m0 += dm0;
+        a.sd_m2 += dm2;
+        a.sd_m3 += dm3;
+        a.sd_m4 += dm4;
+        a.sq_max += (uint64_t)(dmax * dmax);
+        a.sq_m0 += (uint64_t)(dm0 * dm0);
+        const uint64_t ad2 = (uint64_t)(dm2 < 0 ? -dm2 : dm2);
+        a.sq_m2 += (u128)ad2 * ad2;
+        const double f3 = (double)dm3;
+        a.fq_m3 = fma(f3, f3, a.fq_m3);
+        const double f4 = i128_to_f64_fast(dm4);
+        a.fq_m4 = fma(f4, f4, a.fq_m4);
     }
-    const u128 tx = block_sum_u128<BLOCK>(sx, s_u);
-    const u128 tsd_u = block_sum_u128<BLOCK>((u128)sd, s_u);  // two's complement sum
-    const i128 tsd = (i128)tsd_u;
-    double m2b;
-    if (S <= 3) {
-        const u128 tq = block_sum_u128<BLOCK>(sq, s_u);
-        if (threadIdx.x == 0) {
-            const u128 ad = (u128)(tsd < 0 ? -tsd : tsd);
-            if ((tq >> 103) == 0 && (ad >> 63) == 0) {
-                // R * sum d^2 - (sum d)^2 >= 0, exact in 128 bits (R < 2^25)
-                const u128 num = (u128)(uint64_t)p.n_runs * tq - ad * ad;
-                m2b = u128_to_f64(num) / (double)p.n_runs;
-            } else {
-                const double fsd = u128_to_f64(ad);
-                m2b = u128_to_f64(tq) - fsd * fsd / (double)p.n_runs;
-                if (m2b < 0.0) m2b = 0.0;
-            }
-        }
-    } else {
-        const double tf = block_sum_f64<BLOCK>(fsq, s_f);
-        if (threadIdx.x == 0) {
-            const double fsd = i128_to_f64(tsd);
-            m2b = tf - fsd * fsd / (double)p.n_runs;
-            if (m2b < 0.0) m2b = 0.0;
-        }
-    }
-    if (threadIdx.x == 0) {
-        const double R = (double)p.n_runs;
-        const double mean_b = u128_to_f64(tx) / R;
-        const size_t idx = (size_t)S * (p.M + 1) + n;
-        const double na = (double)*p.count_before;
-        const u128 a = ((u128)p.acc.sum_hi[idx] << 64) | p.acc.sum_lo[idx];
-        const double mean_a = na > 0 ? u128_to_f64(a) / na : 0.0;
+    // block sums (results valid in thread 0)
+    const uint64_t span = bsum_u64<BLOCK>(a.span, s_w);
+    const uint64_t sx_max = bsum_u64<BLOCK>(a.sx_max, s_w);
+    const uint64_t sx_m0 = bsum_u64<BLOCK>(a.sx_m0, s_w);
+    const u128 sx_m2 = block_sum_u128<BLOCK>(a.sx_m2, s_u);
+    const u128 sx_m3 = block_sum_u128<BLOCK>(a.sx_m3, s_u);
+    const u128 sx_m4 = block_sum_u128<BLOCK>(a.sx_m4, s_u);
+    const i128 sd_max = (i128)block_sum_u128<BLOCK>((u128)(i128)a.sd_max, s_u);
+    const i128 sd_m0 = (i128)block_sum_u128<BLOCK>((u128)(i128)a.sd_m0, s_u);
+    const i128 sd_m2 = (i128)block_sum_u128<BLOCK>((u128)(i128)a.sd_m2, s_u);
+    const i128 sd_m3 = (i128)block_sum_u128<BLOCK>((u128)a.sd_m3, s_u);
+    const i128 sd_m4 = (i128)block_sum_u128<BLOCK>((u128)a.sd_m4, s_u);
+    const u128 sq_max = block_sum_u128<BLOCK>(a.sq_max, s_u);
+    const u128 sq_m0 = block_sum_u128<BLOCK>(a.sq_m0, s_u);
+    const u128 sq_m2 = block_sum_u128<BLOCK>(a.sq_m2, s_u);
+    const double fq_m3 = block_sum_f64<BLOCK>(a.fq_m3, s_f);
+    const double fq_m4 = block_sum_f64<BLOCK>(a.fq_m4, s_f);
+    if (threadIdx.x != 0) return;
+    const double R = (double)p.n_runs;
+    const uint64_t Rn = (uint64_t)p.n_runs;
+    // exact M2 numerator R * sum d^2 - (sum d)^2 when it fits in 128 bits
+    auto m2_exact = [&](u128 sq, i128 sd) -> double {
+        const u128 ad = (u128)(sd < 0 ? -sd : sd);
+        if ((sq >> 103) == 0 && (ad >> 63) == 0) return u128_to_f64(Rn * sq - ad * ad) / R;
+        const double f = u128_to_f64(ad);
+        const double v = u128_to_f64(sq) - f * f / R;
+        return v > 0.0 ? v : 0.0;
+    };
+    auto m2_float = [&](double fq, i128 sd) -> double {
+        const double f = i128_to_f64(sd);
+        const double v = fq - f * f / R;
+        return v > 0.0 ? v : 0.0;
+    };
+    // statistic order 0 max, 1 m0, 2 m1 (= N - max: same M2 as max), 3 m2, 4 m3, 5 m4
+    const u128 sx[6] = {sx_max, sx_m0, (u128)Rn * p.N - sx_max, sx_m2, sx_m3, sx_m4};
+    const double m2b_max = m2_exact(sq_max, sd_max);
+    const double m2b[6] = {m2b_max, m2_exact(sq_m0, sd_m0), m2b_max, m2_exact(sq_m2, sd_m2),
+                           m2_float(fq_m3, sd_m3), m2_float(fq_m4, sd_m4)};
+    const double na = (double)*p.count_before;
+    for (int k = 0; k < 6; ++k) {
+        const size_t idx = (size_t)k * (p.M + 1) + n;
+        const u128 acc = ((u128)p.acc.sum_hi[idx] << 64) | p.acc.sum_lo[idx];
+        const double mean_a = na > 0 ? u128_to_f64(acc) / na : 0.0;
         double nn = na, mm = mean_a, ss = p.acc.m2[idx];
-        chan_merge(nn, mm, ss, R, mean_b, m2b);
-        const u128 t = a + tx;
+        chan_merge(nn, mm, ss, R, u128_to_f64(sx[k]) / R, m2b[k]);
+        const u128 t = acc + sx[k];
         p.acc.sum_lo[idx] = (uint64_t)t;
         p.acc.sum_hi[idx] = (uint64_t)(t >> 64);
         p.acc.m2[idx] = ss;
     }
-}
-
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
-    const uint32_t n = p.n_begin + blockIdx.x;
-    const int s = blockIdx.y;
-    const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;
-    __shared__ u128 s_u[BLOCK / 32];
-    __shared__ double s_f[BLOCK / 32];
-    if (s == 6) {
-        uint32_t c = 0;
-        for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) c += (p.rec.max_span[row + r] >> 31);
-        const u128 t = block_sum_u128<BLOCK>(c, s_u);
-        if (threadIdx.x == 0) p.acc.span_count[n] += (uint64_t)t;
-        return;
-    }
-    switch (s) {
-        case 0: micro_stat<BLOCK, 0>(p, n, row, s_u, s_f); break;
-        case 1: micro_stat<BLOCK, 1>(p, n, row, s_u, s_f); break;
-        case 2: micro_stat<BLOCK, 2>(p, n, row, s_u, s_f); break;
-        case 3: micro_stat<BLOCK, 3>(p, n, row, s_u, s_f); break;
-        case 4: micro_stat<BLOCK, 4>(p, n, row, s_u, s_f); break;
-        default: micro_stat<BLOCK, 5>(p, n, row, s_u, s_f); break;
-    }
+    p.acc.span_count[n] += span;
 }
 
 void launch_micro_window(const MicroParams &p, cudaStream_t s) {
-    dim3 grid(p.n_end - p.n_begin, 7);
-    if (grid.x == 0 || p.n_runs <= 0) return;
-    micro_window_kernel<256><<<grid, 256, 0, s>>>(p);
+    const uint32_t rows = p.n_end - p.n_begin;
+    if (rows == 0 || p.n_runs <= 0) return;
+    micro_window_kernel<256><<<rows, 256, 0, s>>>(p);
 }
 
 void launch_micro_count(uint64_t *count, int32_t n_runs, cudaStream_t s) {
@@ -750,7 +796,7 @@ __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, 
     const int map[6] = {0, 1, 2, 3, 4, 5};  // max, m0, m1, m2, m3, m4
     for (int j = 0; j < 6; ++j) {
         const size_t idx = (size_t)map[j] * (M + 1) + n;
-        const double mean = (ldexp((double)acc.sum_hi[idx], 64) + (double)acc.sum_lo[idx]) / R;
+        const double mean = fma((double)acc.sum_hi[idx], 18446744073709551616.0, (double)acc.sum_lo[idx]) / R;
         const double m2 = acc.m2[idx];
         const double sd = R > 1.0 ? sqrt(m2 / (R - 1.0)) : NAN;
         double lo = mean, hi = mean;

@@ -254,8 +254,7 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
 
 constexpr int kConvRuns = 128;  // runs per CTA (one per thread)
 constexpr int kConvPT = 16;     // probabilities per CTA
-constexpr int kConvChunk = 64;  // rows staged per step
-constexpr int kConvFlush = 8;   // chunks summed in FP32 before an FP64 flush
+constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before an FP64 flush
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
 // kConvPT canonical values of its run for one statistic over the window's
@@ -265,7 +264,7 @@ constexpr int kConvFlush = 8;   // chunks summed in FP32 before an FP64 flush
 template <int PRECISION, int S>
 __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                           const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
-                                          typename std::conditional<PRECISION == 0, double, float>::type *mid) {
+                                          double *acc) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     wtype part[kConvPT];
 #pragma unroll
@@ -279,7 +278,7 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
         for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
     }
 #pragma unroll
-    for (int j = 0; j < kConvPT; ++j) mid[j] += part[j];
+    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
 }
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
@@ -314,13 +313,9 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = s_range[0], nhi = s_range[1];
     if (nlo >= nhi) return;
-    // sums: FP32 over kConvChunk rows (part), FP32 over kConvFlush chunks
-    // (mid), FP64 beyond (acc); FP64 is a small fraction of the issue slots
     double acc[kConvPT];
-    wtype mid[kConvPT];
 #pragma unroll
-    for (int j = 0; j < kConvPT; ++j) { acc[j] = 0.0; mid[j] = 0; }
-    int chunk = 0;
+    for (int j = 0; j < kConvPT; ++j) acc[j] = 0.0;
     for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
         const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
         __syncthreads();
@@ -337,23 +332,16 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
         __syncthreads();
         if (r < p.n_runs) {
             switch (s) {
-                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, mid); break;
-                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, mid); break;
-                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, mid); break;
-                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, mid); break;
-                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, mid); break;
-                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, mid); break;
-                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, mid); break;
-            }
-            if (++chunk == kConvFlush) {
-                chunk = 0;
-#pragma unroll
-                for (int j = 0; j < kConvPT; ++j) { acc[j] += (double)mid[j]; mid[j] = 0; }
+                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, acc); break;
+                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, acc); break;
+                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, acc); break;
+                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, acc); break;
+                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, acc); break;
+                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, acc); break;
+                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, acc); break;
             }
         }
     }
-#pragma unroll
-    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)mid[j];
     if (r < p.n_runs) {
 #pragma unroll
         for (int j = 0; j < kConvPT; ++j) {
@@ -500,7 +488,6 @@ __device__ __forceinline__ double i128_to_f64(i128 x) {
     return x < 0 ? -u128_to_f64((u128)(-x)) : u128_to_f64((u128)x);
 }
 
-constexpr double kTwo64 = 18446744073709551616.0;
 constexpr double kTwo32 = 4294967296.0;
 
 // Per-thread partial sums of one row: for every statistic the exact sum of

@@ -66,15 +66,17 @@ void nzo_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2],
 /* ------------------------------------------------------------------ */
 /* Philox-keyed Feistel permutation of [0, M)                          */
 /* ------------------------------------------------------------------ */
-/* Domain 2^(2h) >= M with h = ceil(bits(M-1)/2); 8 rounds; each round
- * F(R) = top h bits of hi32(((R << (32-h)) ^ k_i) * 0xD2511F53).
- * Values >= M are walked (re-encrypted) until they fall inside [0, M),
- * which keeps the map a bijection on [0, M). */
+/* Alternating Feistel network on b = bits(M-1) bits: left part floor(b/2)
+ * bits, right part the rest; even rounds xor the left part with a keyed hash
+ * of the right part, odd rounds the other way round; 8 rounds; the hash of a
+ * v-bit value to o bits is the top o bits of hi32(((v << (32-v)) ^ k) *
+ * 0xD2511F53).  Values >= M are re-encrypted (cycle walking), which keeps
+ * the map a bijection on [0, M). */
 #define NZ_FEISTEL_ROUNDS 8
 #define NZ_PERM_TAG 0x5045524Du /* "PERM" */
 
 typedef struct {
-    uint32_t M, h, mask, pad;
+    uint32_t M, hl, hr, maskL, maskR;
     uint32_t k[NZ_FEISTEL_ROUNDS];
 } nzo_perm_t;
 
@@ -85,12 +87,11 @@ void nzo_perm_init(nzo_perm_t *st, uint64_t key, uint64_t run_id, uint32_t M)
         uint32_t x = M - 1;
         while (x) { ++bits; x >>= 1; }
     }
-    uint32_t h = (bits + 1) / 2;
-    if (h == 0) h = 1;
     st->M = M;
-    st->h = h;
-    st->mask = (1u << h) - 1u;
-    st->pad = 0;
+    st->hl = bits / 2;
+    st->hr = bits - st->hl;
+    st->maskL = (1u << st->hl) - 1u;
+    st->maskR = (1u << st->hr) - 1u;
     uint32_t kk[2] = {(uint32_t)key, (uint32_t)(key >> 32)};
     for (uint32_t half = 0; half < 2; ++half) {
         uint32_t ctr[4] = {(uint32_t)run_id, (uint32_t)(run_id >> 32), half,
@@ -99,18 +100,21 @@ void nzo_perm_init(nzo_perm_t *st, uint64_t key, uint64_t run_id, uint32_t M)
     }
 }
 
+static inline uint32_t nzo_feistel_f(uint32_t v, uint32_t vbits, uint32_t obits, uint32_t k)
+{
+    uint32_t in = (vbits ? (v << (32u - vbits)) : 0u) ^ k;
+    uint32_t h = (uint32_t)(((uint64_t)in * PHILOX_M0) >> 32);
+    return obits ? (h >> (32u - obits)) : 0u;
+}
+
 static inline uint32_t nzo_feistel(const nzo_perm_t *st, uint32_t x)
 {
-    uint32_t h = st->h, mask = st->mask;
-    uint32_t L = x >> h, R = x & mask;
-    for (int i = 0; i < NZ_FEISTEL_ROUNDS; ++i) {
-        uint32_t in = (R << (32 - h)) ^ st->k[i];
-        uint32_t f = (uint32_t)(((uint64_t)in * PHILOX_M0) >> 32) >> (32 - h);
-        uint32_t nl = R;
-        R = L ^ (f & mask);
-        L = nl;
+    uint32_t L = x >> st->hr, R = x & st->maskR;
+    for (int i = 0; i < NZ_FEISTEL_ROUNDS; i += 2) {
+        L ^= nzo_feistel_f(R, st->hr, st->hl, st->k[i]) & st->maskL;
+        R ^= nzo_feistel_f(L, st->hl, st->hr, st->k[i + 1]) & st->maskR;
     }
-    return (L << h) | R;
+    return (L << st->hr) | R;
 }
 
 uint32_t nzo_perm_at(const nzo_perm_t *st, uint32_t n)

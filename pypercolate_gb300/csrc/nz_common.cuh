@@ -57,11 +57,24 @@ __host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 }
 
 // ------------------------------------------------------- Feistel permutation
+// Alternating Feistel network on exactly b = bits(M - 1) bits, split into a
+// left part of floor(b/2) bits and a right part of the remaining bits; round
+// i xors one part with a keyed hash of the other (even rounds update the
+// left part, odd rounds the right part), 8 rounds, round keys from two
+// Philox-4x32-10 blocks.  Values >= M are re-encrypted (cycle walking); the
+// domain is < 2M so fewer than 2 walks are needed on average, and about one
+// for spanning_2d_grid(2^k), whose M = 2L(L-1) lies just below 2^b.
 constexpr int kFeistelRounds = 8;
 constexpr uint32_t kPermTag = 0x5045524Du;  // "PERM"
 
+__host__ __device__ __forceinline__ uint32_t feistel_f(uint32_t v, uint32_t vbits, uint32_t obits, uint32_t k) {
+    const uint32_t in = (vbits ? (v << (32u - vbits)) : 0u) ^ k;
+    const uint32_t h = (uint32_t)(((uint64_t)in * kPhiloxM0) >> 32);
+    return obits ? (h >> (32u - obits)) : 0u;
+}
+
 struct FeistelPerm {
-    uint32_t M, h, mask;
+    uint32_t M, hl, hr, maskL, maskR;
     uint32_t k[kFeistelRounds];
 
     __host__ __device__ void init(uint64_t key, uint64_t run_id, uint32_t m) {
@@ -70,9 +83,11 @@ struct FeistelPerm {
             uint32_t x = m - 1;
             while (x) { ++bits; x >>= 1; }
         }
-        uint32_t hh = (bits + 1) / 2;
-        if (hh == 0) hh = 1;
-        M = m; h = hh; mask = (1u << hh) - 1u;
+        M = m;
+        hl = bits / 2;
+        hr = bits - hl;
+        maskL = (1u << hl) - 1u;
+        maskR = (1u << hr) - 1u;
 #pragma unroll
         for (uint32_t half = 0; half < 2; ++half) {
             uint32_t c[4] = {(uint32_t)run_id, (uint32_t)(run_id >> 32), half, kPermTag};
@@ -83,17 +98,13 @@ struct FeistelPerm {
     }
 
     __host__ __device__ __forceinline__ uint32_t encrypt(uint32_t x) const {
-        uint32_t L = x >> h, R = x & mask;
-        const uint32_t sh = 32u - h;
+        uint32_t L = x >> hr, R = x & maskR;
 #pragma unroll
-        for (int i = 0; i < kFeistelRounds; ++i) {
-            uint32_t in = (R << sh) ^ k[i];
-            uint32_t f = (uint32_t)(((uint64_t)in * kPhiloxM0) >> 32) >> sh;
-            uint32_t nl = R;
-            R = L ^ (f & mask);
-            L = nl;
+        for (int i = 0; i < kFeistelRounds; i += 2) {
+            L ^= feistel_f(R, hr, hl, k[i]) & maskL;
+            R ^= feistel_f(L, hl, hr, k[i + 1]) & maskR;
         }
-        return (L << h) | R;
+        return (L << hr) | R;
     }
 
     // n-th element of the permutation of [0, M) (requires n < M).

@@ -72,6 +72,11 @@ __global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
     else perm = p.perms + (size_t)r * g.M;
 
     const NzRecords rec = p.rec;
+    // powers of the largest cluster size, recomputed only when it grows
+    uint32_t mx = st.max;
+    uint64_t mx2 = (uint64_t)mx * mx;
+    uint64_t mx3 = mx2 * mx;
+    uint64_t mx4_lo = mx3 * mx, mx4_hi = __umul64hi(mx3, (uint64_t)mx);
     for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
         uint32_t e = 0;
         if (n > 0) {
@@ -116,15 +121,17 @@ __global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
                 st.t3 += 3ull * ab * s;
                 const uint64_t q = 4ull * a * a + 6ull * ab + 4ull * b * b;
                 add128(st.t4_lo, st.t4_hi, ab * q, __umul64hi(ab, q));
-                if (s > st.max) st.max = s;
+                if (s > mx) {
+                    mx = s;
+                    mx2 = (uint64_t)mx * mx;
+                    mx3 = mx2 * mx;
+                    mx4_lo = mx3 * mx;
+                    mx4_hi = __umul64hi(mx3, (uint64_t)mx);
+                }
                 if (SPAN && (sides == 3u || (st.flags & kFlagInitBoth))) st.flags |= kFlagSpan;
             }
         }
         // row n: moments = T_k - max^k
-        const uint32_t mx = st.max;
-        const uint64_t mx2 = (uint64_t)mx * mx;
-        const uint64_t mx3 = mx2 * mx;
-        const uint64_t mx4_lo = mx3 * mx, mx4_hi = __umul64hi(mx3, (uint64_t)mx);
         const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
         if (rec.max_span) rec.max_span[off] = mx | ((SPAN && (st.flags & kFlagSpan)) ? kSpanBit : 0u);
         if (rec.m0) rec.m0[off] = st.t0 - 1u;
@@ -136,6 +143,7 @@ __global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
         if (rec.m4_hi) rec.m4_hi[off] = (uint32_t)m4_hi;
         if (rec.edge) rec.edge[off] = e;
     }
+    st.max = mx;
     p.state[r] = st;
 }
 

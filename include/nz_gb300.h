@@ -107,6 +107,32 @@ int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs,
                       void *workspace, size_t workspace_bytes,
                       const NzRecords *out, void *stream);
 
+/* Same computation as nz_microcanonical, for callers that cannot allocate
+ * device memory (a host framework that owns the whole device pool, or a
+ * foreign-language binding that can only pass buffers it already holds).
+ * The scratch nz_microcanonical takes as `workspace` lives instead in a
+ * fixed 64 MiB array inside the library (nz_static_scratch_bytes()), which
+ * every GPU that loads the library reserves until the process exits; calls
+ * needing more (nz_microcanonical_workspace_bytes() > 64 MiB, e.g. more than
+ * 255 runs of spanning_2d_grid(256)) return NZ_ERR_TOO_LARGE.  No cudaMalloc,
+ * cudaFree or allocating library routine is called (keep the nz_profile_*
+ * instrumentation off on this path: when on, it creates CUDA event objects).
+ * The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * Every call shares the one array, which keeps the previous call's contents:
+ * calls whose execution overlaps on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.
+ * (No counterpart in the reference.) */
+int nz_microcanonical_noalloc(const NzGraph *graph, int32_t spanning,
+                              int32_t n_runs, int32_t perm_mode, uint64_t key,
+                              uint64_t run0, const uint32_t *perms,
+                              const uint32_t *mt_seed_words,
+                              const int32_t *mt_seed_len,
+                              int32_t mt_words_stride, const NzRecords *out,
+                              void *stream);
+size_t nz_static_scratch_bytes(void);
+
 /* Writes the permutations the runs would use (for checking and for
  * NZ_PERM_GIVEN replays): out[r * M + n]. */
 int nz_permutations(uint32_t num_edges, int32_t n_runs, int32_t perm_mode,

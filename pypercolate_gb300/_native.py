@@ -64,6 +64,11 @@ _SIGNATURES = [
      [ctypes.POINTER(NzGraph), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
       ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp, ctypes.c_int32, _vp,
       ctypes.c_size_t, ctypes.POINTER(NzRecords), _vp]),
+    ('nz_microcanonical_noalloc', ctypes.c_int,
+     [ctypes.POINTER(NzGraph), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+      ctypes.c_uint64, ctypes.c_uint64, _vp, _vp, _vp, ctypes.c_int32,
+      ctypes.POINTER(NzRecords), _vp]),
+    ('nz_static_scratch_bytes', ctypes.c_size_t, []),
     ('nz_permutations', ctypes.c_int,
      [ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_uint64,
       _vp, _vp, ctypes.c_int32, _vp, _vp]),

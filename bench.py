@@ -48,6 +48,9 @@ def parse():
     ap.add_argument('--window', type=int, default=0)
     ap.add_argument('--cpu-sample', type=int, default=256, help='runs in the CPU baseline sample')
     ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--plain-runs', type=int, default=8192,
+                    help='runs timed on the plain path (0: skip)')
+    ap.add_argument('--plain-chunk', type=int, default=4096)
     ap.add_argument('--l2-fetch', type=int, default=32,
                     help='L2 fetch granularity of this process (bytes; 0 = leave as is)')
     return ap.parse_args()
@@ -244,6 +247,30 @@ def main():
     kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 1, 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
+    # plain GPU path (one lattice per launch): chunks of runs whose records for
+    # all M+1 rows are materialised by one union-find launch, FP64 convolution
+    plain = None
+    if args.plain_runs > 0:
+        chunk = min(args.plain_chunk, args.plain_runs)
+        pe = Ensemble('grid', L, ps, precision='fp64', micro=not args.no_micro, window=M + 1)
+        pe.run(chunk, key=KEY, run0=run_base + 2 * 10 ** 8)  # warm-up
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        done = 0
+        while done < args.plain_runs:
+            pe.run(chunk, key=KEY, run0=run_base + 3 * 10 ** 8 + done)
+            done += chunk
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        plain = {'value': done * M / (pms * 1e-3), 'unit': 'bond additions/s', 'runs': done,
+                 'chunk': chunk, 'ms': pms,
+                 'path': 'records for all M+1 rows per launch, FP64 convolution'}
+        del pe
+        torch.cuda.empty_cache()
+
     # end to end through the public API: inputs (p-grid) from pinned host
     # memory, results (finalized canonical averages) read back every step
     h_ps = torch.from_numpy(ps.copy()).pin_memory()
@@ -282,6 +309,8 @@ def main():
                      'bytes_per_addition': UF_BYTES_PER_ADD,
                      'avg_launch_ms': uf_avg_s * 1e3},
         'kernel_ms_per_step': {k: v[1] / args.steps for k, v in prof.items()},
+        'plain_gpu': plain,
+        'batched_vs_plain': (value / world / plain['value']) if plain else None,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
         'e2e': {'value': e2e_value, 'unit': 'bond additions/s', 'h2d_bytes_per_step': h2d,

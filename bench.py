@@ -51,6 +51,10 @@ def parse():
     ap.add_argument('--plain-runs', type=int, default=8192,
                     help='runs timed on the plain path (0: skip)')
     ap.add_argument('--plain-chunk', type=int, default=4096)
+    ap.add_argument('--mix-runs', type=int, default=1000000,
+                    help='runs of the batched uneven workload (0: skip)')
+    ap.add_argument('--study', default=None, choices=[None, 'precision'],
+                    help='precision: FP32 vs FP64 canonical curves at L=1024 (separate line)')
     ap.add_argument('--l2-fetch', type=int, default=32,
                     help='L2 fetch granularity of this process (bytes; 0 = leave as is)')
     return ap.parse_args()
@@ -180,10 +184,66 @@ def run_reference(args):
     return 0
 
 
+STAT_NAMES = ('percolation_probability', 'max_cluster_size', 'm0', 'm1', 'm2', 'm3', 'm4')
+
+
+def precision_study(args):
+    """Canonical curves of spanning_2d_grid(L) from FP32 (FP64 chunk sums)
+    against FP64 convolution of the same exact records (same Philox runs):
+    max absolute and relative error per curve.  Default: L=1024, 2e4 runs,
+    1000 uniform p in [0, 1] + 1000 uniform p in [0.48, 0.52]."""
+    import torch
+    from pypercolate_gb300 import _native as nat
+    from pypercolate_gb300.ensemble import Ensemble
+    torch.cuda.set_device(0)
+    if args.l2_fetch:
+        nat.set_l2_fetch_granularity(args.l2_fetch)
+    L = args.L if args.L != L_DEFAULT else 1024
+    R = args.runs if args.runs != 100000 else 20000
+    ps = np.concatenate([np.linspace(0.0, 1.0, 1000), np.linspace(0.48, 0.52, 1000)])
+    N = L * L
+    out = {}
+    times = {}
+    for prec in ('fp64', 'fp32'):
+        e = Ensemble('grid', L, ps, precision=prec, micro=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        chunk = min(R, 20000)
+        done = 0
+        while done < R:
+            e.run(min(chunk, R - done), key=KEY, run0=done)
+            done += min(chunk, R - done)
+        torch.cuda.synchronize()
+        times[prec] = time.perf_counter() - t0
+        ca = e.canonical_averages()
+        out[prec] = np.column_stack([ca['percolation_probability_mean'],
+                                     ca['max_cluster_size_mean'], ca['moments_mean']])
+        del e
+        torch.cuda.empty_cache()
+    ref, got = out['fp64'], out['fp32']
+    norm = np.array([1.0, N, N, N, N, N, N])  # curves as the finalised output reports them
+    err = {}
+    for j, name in enumerate(STAT_NAMES):
+        a = np.abs(got[:, j] - ref[:, j]) / norm[j]
+        rel = np.abs(got[:, j] - ref[:, j]) / np.maximum(np.abs(ref[:, j]), 1e-300)
+        err[name] = {'max_abs': float(a.max()), 'max_rel': float(rel[np.abs(ref[:, j]) > 0].max())
+                     if np.any(np.abs(ref[:, j]) > 0) else 0.0}
+    line = {'study': 'canonical precision', 'L': L, 'runs': R, 'P': len(ps),
+            'p_grid': '1000 uniform in [0,1] + 1000 uniform in [0.48,0.52]',
+            'compare': 'FP32 products/chunk sums (FP64 across 128-row chunks) vs FP64 '
+                       'convolution of the same exact per-step records',
+            'normalisation': 'spanning as is; max and moments divided by N (finalised curves)',
+            'errors': err, 'seconds': times}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.study == 'precision':
+        return precision_study(args)
     import torch
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
@@ -271,6 +331,37 @@ def main():
         del pe
         torch.cuda.empty_cache()
 
+    # batched uneven workload: 10^6 runs, 2D L log-uniform in [8, 512] and
+    # chains l log-uniform in [1024, 65536], 50/50, one persistent launch per
+    # ensemble replayed as a CUDA graph; launch shape from the autotuner
+    mix = None
+    if args.mix_runs > 0:
+        from pypercolate_gb300.autotune import tune_mix
+        from pypercolate_gb300.mix import MixEnsemble
+        tuned = tune_mix(args.mix_runs, cache_path=None)
+        threads, block, smem = tuned['best']
+        me = MixEnsemble(args.mix_runs, threads=threads, block=block, smem_words=smem)
+        me.capture()
+        me.replay(7)
+        torch.cuda.synchronize()
+        m0e = torch.cuda.Event(enable_timing=True)
+        m1e = torch.cuda.Event(enable_timing=True)
+        m0e.record(stream)
+        for k in range(2):
+            me.replay(8 + k)
+        m1e.record(stream)
+        torch.cuda.synchronize()
+        mms = m0e.elapsed_time(m1e) / 2
+        adds = me.additions
+        mix = {'value': adds / (mms * 1e-3), 'unit': 'bond additions/s', 'runs': args.mix_runs,
+               'additions_per_ensemble': adds, 'ms_per_ensemble': mms,
+               'launch': {'threads': threads, 'block': block, 'smem_words': smem},
+               'autotune': [list(t) for t in tuned['table']], 'cuda_graph': True,
+               'workload': '2D L log-uniform [8,512] + chains l log-uniform [1024,65536], '
+                           '50/50, 256 checkpoints, exact per-lattice reductions'}
+        del me
+        torch.cuda.empty_cache()
+
     # end to end through the public API: inputs (p-grid) from pinned host
     # memory, results (finalized canonical averages) read back every step
     h_ps = torch.from_numpy(ps.copy()).pin_memory()
@@ -310,6 +401,7 @@ def main():
                      'avg_launch_ms': uf_avg_s * 1e3},
         'kernel_ms_per_step': {k: v[1] / args.steps for k, v in prof.items()},
         'plain_gpu': plain,
+        'batched_uneven': mix,
         'batched_vs_plain': (value / world / plain['value']) if plain else None,
         'clocks': clocks,
         'gpu_launches': gpu_launches,

@@ -225,7 +225,26 @@ typedef struct NzMicroAccum {
  * hi) divided by num_nodes, Student-t intervals ((mean, mean) if std == 0). */
 int nz_microcanonical_finalize(const NzMicroAccum *acc, uint32_t num_nodes,
                                uint32_t num_edges, int32_t spanning,
-                               double alpha, double *out, void *stream);
+                               double alpha, int32_t normalize, double *out,
+                               void *stream);
+/* (normalize = 0: absolute units as microcanonical_averages yields them,
+ * percolate/percolate.py:708-896; 1: divided by N as in the arrays.) */
+
+/* Adds the runs of a record set (rows n_begin..n_end-1 of all its runs; the
+ * records' row 0 is n_begin) to the accumulators: the run-reductions of
+ * percolate/percolate.py:450-705 at every n. */
+int nz_microcanonical_reduce(const NzRecords *rec, uint32_t num_nodes,
+                             uint32_t num_edges, int32_t n_runs,
+                             uint32_t n_begin, uint32_t n_end,
+                             const NzMicroAccum *acc, void *stream);
+
+/* Continues numpy's global MT19937 stream: state_in = 624 key words + the
+ * position (np.random.get_state()); draws n_runs permutations of range(M) in
+ * order, as the classic API's runs draw np.random.permutation(M)
+ * (percolate/percolate.py:270); writes the advanced state to state_out. */
+int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
+                              int32_t n_runs, uint32_t *out,
+                              uint32_t *state_out, void *stream);
 
 /* The whole per-lattice pipeline for n_runs Philox runs:
  * permutation -> union-find -> (optional) fused microcanonical reductions
@@ -241,6 +260,50 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
                 void *workspace, size_t workspace_bytes, uint64_t *acc_count,
                 double *acc_mean, double *acc_m2, const NzMicroAccum *micro,
                 void *stream);
+
+/* ---- batched uneven ensembles (one persistent launch) ------------------ */
+/* Run r draws its substrate from Philox-4x32-10 (key, counter r): a chain
+ * with probability chain_share / 2^32, else a square lattice; the length L
+ * (or l) is the largest grid_min + i (chain_min + i) with thr[i] <= u, u a
+ * uniform 32-bit word, thr[0] = 0.  For a log-uniform length rounded to the
+ * nearest integer, thr[i] = ceil(2^32 ln((len - 1/2) / min) / ln(max / min)).
+ * Runs of every lattice (kind, length) = "class" are reduced at `checkpoints`
+ * occupation numbers n_j = floor(j M / (checkpoints - 1)), j = 0..F-1, to
+ * exact integer sums and exact-numerator M2 of max, m0, m1, m2, m3, m4 and
+ * spanning counts (percolate/percolate.py:450-705 statistics at those n). */
+typedef struct NzMixSpec {
+    uint32_t grid_min, grid_max;   /* spanning_2d_grid lengths (inclusive)   */
+    uint32_t chain_min, chain_max; /* spanning_1d_chain lengths (inclusive)  */
+    uint32_t chain_share;          /* P(chain) * 2^32                         */
+    int32_t checkpoints;           /* F >= 2                                  */
+} NzMixSpec;
+
+/* Per class c (grid classes first: c = L - grid_min; then chains:
+ * c = n_grid + l - chain_min) and checkpoint j; arrays over [class][F],
+ * sums/m2 over [6][class][F] with statistic order max, m0, m1, m2, m3, m4. */
+typedef struct NzMixAccum {
+    uint32_t *count;   /* [classes] runs in the class                        */
+    uint32_t *span;    /* [classes][F] runs with a spanning cluster          */
+    uint64_t *sum_lo;  /* [6][classes][F] exact sums, low words              */
+    uint64_t *sum_hi;  /* high words                                         */
+    double *m2;        /* [6][classes][F] sums of squared deviations         */
+    uint32_t *errors;  /* [1] runs skipped by a failed internal check (0)    */
+} NzMixAccum;
+
+/* Workspace for n_runs runs and `threads` persistent threads; each thread's
+ * node slot is sized for the largest lattice of the spec. */
+size_t nz_mix_workspace_bytes(const NzMixSpec *spec, int32_t n_runs,
+                              int32_t threads);
+/* key_dev: device pointer to the Philox key (read by the kernels, so a
+ * captured CUDA graph of this call can be replayed with another key).
+ * threads: persistent threads; block: threads per CTA; smem_words: per-thread
+ * shared-memory node slot (0 = none) -- runs with N <= smem_words use it.
+ * Output arrays are overwritten (not accumulated). */
+int nz_mix(const NzMixSpec *spec, const uint32_t *thr_grid,
+           const uint32_t *thr_chain, const uint64_t *key_dev, int32_t n_runs,
+           int32_t threads, int32_t block, uint32_t smem_words,
+           void *workspace, size_t workspace_bytes, const NzMixAccum *out,
+           void *stream);
 
 /* ---- memory-system hint ------------------------------------------------ */
 /* L2 fetch granularity of the calling CUDA context (cudaLimitMaxL2FetchGranularity:

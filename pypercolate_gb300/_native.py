@@ -53,6 +53,17 @@ class NzMicroAccum(ctypes.Structure):
                 ('sum_hi', _vp), ('m2', _vp)]
 
 
+class NzMixSpec(ctypes.Structure):
+    _fields_ = [('grid_min', ctypes.c_uint32), ('grid_max', ctypes.c_uint32),
+                ('chain_min', ctypes.c_uint32), ('chain_max', ctypes.c_uint32),
+                ('chain_share', ctypes.c_uint32), ('checkpoints', ctypes.c_int32)]
+
+
+class NzMixAccum(ctypes.Structure):
+    _fields_ = [('count', _vp), ('span', _vp), ('sum_lo', _vp), ('sum_hi', _vp), ('m2', _vp),
+                ('errors', _vp)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _SIGNATURES = [
     ('nz_version', ctypes.c_char_p, []),
@@ -95,8 +106,18 @@ _SIGNATURES = [
       _vp]),
     ('nz_microcanonical_finalize', ctypes.c_int,
      [ctypes.POINTER(NzMicroAccum), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
-      ctypes.c_double, _vp, _vp]),
+      ctypes.c_double, ctypes.c_int32, _vp, _vp]),
+    ('nz_microcanonical_reduce', ctypes.c_int,
+     [ctypes.POINTER(NzRecords), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
+      ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(NzMicroAccum), _vp]),
+    ('nz_mt_stream_permutations', ctypes.c_int,
+     [_vp, ctypes.c_uint32, ctypes.c_int32, _vp, _vp, _vp]),
     ('nz_student_t_quantile', ctypes.c_int, [_vp, _vp, ctypes.c_int32, _vp, _vp]),
+    ('nz_mix_workspace_bytes', ctypes.c_size_t,
+     [ctypes.POINTER(NzMixSpec), ctypes.c_int32, ctypes.c_int32]),
+    ('nz_mix', ctypes.c_int,
+     [ctypes.POINTER(NzMixSpec), _vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32,
+      ctypes.c_int32, ctypes.c_uint32, _vp, ctypes.c_size_t, ctypes.POINTER(NzMixAccum), _vp]),
     ('nz_set_l2_fetch_granularity', ctypes.c_int, [ctypes.c_int32]),
     ('nz_get_l2_fetch_granularity', ctypes.c_int, [_vp]),
     ('nz_profile_enable', None, [ctypes.c_int32]),

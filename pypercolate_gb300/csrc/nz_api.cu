@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -300,11 +301,40 @@ int nz_finalize_canonical_averages(const uint8_t *avg_rows, int32_t P, int32_t s
 }
 
 int nz_microcanonical_finalize(const NzMicroAccum *acc, uint32_t num_nodes, uint32_t num_edges, int32_t spanning,
-                               double alpha, double *out, void *stream) {
+                               double alpha, int32_t normalize, double *out, void *stream) {
     if (!acc || !out || !acc->count || !acc->span_count || !acc->sum_lo || !acc->sum_hi || !acc->m2)
         return NZ_ERR_INVALID;
     if (!(alpha > 0.0 && alpha < 1.0)) return NZ_ERR_INVALID;
-    launch_micro_finalize(*acc, num_nodes, num_edges, spanning, alpha, out, as_stream(stream));
+    launch_micro_finalize(*acc, num_nodes, num_edges, spanning, alpha, normalize, out, as_stream(stream));
+    return check_launch();
+}
+
+int nz_microcanonical_reduce(const NzRecords *rec, uint32_t num_nodes, uint32_t num_edges, int32_t n_runs,
+                             uint32_t n_begin, uint32_t n_end, const NzMicroAccum *acc, void *stream) {
+    if (!rec || !acc || n_runs <= 0 || n_end <= n_begin || n_end > num_edges + 1) return NZ_ERR_INVALID;
+    if (!rec->max_span || !rec->m0 || !rec->m2 || !rec->m3 || !rec->m4_lo || !rec->m4_hi ||
+        rec->run_stride < n_runs)
+        return NZ_ERR_INVALID;
+    if (!acc->count || !acc->span_count || !acc->sum_lo || !acc->sum_hi || !acc->m2) return NZ_ERR_INVALID;
+    MicroParams mp;
+    mp.rec = *rec;
+    mp.n_begin = n_begin;
+    mp.n_end = n_end;
+    mp.N = num_nodes;
+    mp.n_runs = n_runs;
+    mp.acc = *acc;
+    mp.M = num_edges;
+    mp.count_before = acc->count;
+    cudaStream_t s = as_stream(stream);
+    launch_micro_window(mp, s);
+    launch_micro_count(acc->count, n_runs, s);
+    return check_launch();
+}
+
+int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges, int32_t n_runs, uint32_t *out,
+                              uint32_t *state_out, void *stream) {
+    if (!state_in || !state_out || n_runs <= 0 || (num_edges > 0 && !out)) return NZ_ERR_INVALID;
+    launch_mt_stream_perms(state_in, num_edges, n_runs, out, state_out, as_stream(stream));
     return check_launch();
 }
 
@@ -465,6 +495,90 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         launch_reduce_runs(L.stats, n_runs, P, acc_count, acc_mean, acc_m2, L.part, L.slices, s);
     }
     return check_launch();
+}
+
+// --------------------------------------------------------- batched uneven
+namespace {
+
+int mix_validate(const NzMixSpec *spec, int32_t n_runs, int32_t threads) {
+    if (!spec || n_runs <= 0 || threads <= 0) return NZ_ERR_INVALID;
+    if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
+    if (spec->grid_min < 1 || spec->grid_max < spec->grid_min || spec->chain_min < 1 ||
+        spec->chain_max < spec->chain_min || spec->checkpoints < 2)
+        return NZ_ERR_INVALID;
+    if ((uint64_t)spec->grid_max * spec->grid_max > NZ_MAX_NODES || spec->chain_max > NZ_MAX_NODES)
+        return NZ_ERR_TOO_LARGE;
+    return NZ_OK;
+}
+
+size_t mix_layout(Carver &c, const NzMixSpec &sp, int32_t n_runs, int32_t T, MixLaunch &L) {
+    const uint32_t n_classes = (sp.grid_max - sp.grid_min + 1) + (sp.chain_max - sp.chain_min + 1);
+    const uint64_t nmax = std::max<uint64_t>((uint64_t)sp.grid_max * sp.grid_max, sp.chain_max);
+    const size_t F = (size_t)sp.checkpoints;
+    L.cls = c.take<uint32_t>(n_runs);
+    L.counts = c.take<uint32_t>(n_classes);
+    L.order = c.take<uint32_t>(n_classes);
+    L.offsets = c.take<uint32_t>(n_classes);
+    L.cursor = c.take<uint32_t>(n_classes);
+    L.queue = c.take<uint32_t>(n_runs);
+    L.head = c.take<uint32_t>(1);
+    L.slot_off = c.take<uint64_t>((size_t)T + 1);
+    L.nodes = c.take<uint32_t>((size_t)T * nmax);
+    L.rec.max_span = c.take<uint32_t>((size_t)n_runs * F);
+    L.rec.m0 = c.take<uint32_t>((size_t)n_runs * F);
+    L.rec.m2 = c.take<uint64_t>((size_t)n_runs * F);
+    L.rec.m3 = c.take<uint64_t>((size_t)n_runs * F);
+    L.rec.m4_lo = c.take<uint64_t>((size_t)n_runs * F);
+    L.rec.m4_hi = c.take<uint32_t>((size_t)n_runs * F);
+    return c.used;
+}
+
+}  // namespace
+
+size_t nz_mix_workspace_bytes(const NzMixSpec *spec, int32_t n_runs, int32_t threads) {
+    if (mix_validate(spec, n_runs, threads) != NZ_OK) return 0;
+    Carver c{nullptr, 0, 0};
+    MixLaunch L;
+    return align_up(mix_layout(c, *spec, n_runs, threads, L));
+}
+
+int nz_mix(const NzMixSpec *spec, const uint32_t *thr_grid, const uint32_t *thr_chain, const uint64_t *key_dev,
+           int32_t n_runs, int32_t threads, int32_t block, uint32_t smem_words, void *workspace,
+           size_t workspace_bytes, const NzMixAccum *out, void *stream) {
+    int st = mix_validate(spec, n_runs, threads);
+    if (st) return st;
+    if (!thr_grid || !thr_chain || !key_dev || !out || !out->count || !out->span || !out->sum_lo ||
+        !out->sum_hi || !out->m2 || !out->errors)
+        return NZ_ERR_INVALID;
+    if (block <= 0 || block > 256 || (block & 31)) return NZ_ERR_INVALID;
+    if ((size_t)smem_words * 4u * (size_t)block > 227u * 1024u) return NZ_ERR_INVALID;
+    Carver c{static_cast<uint8_t *>(workspace), 0, workspace_bytes};
+    MixLaunch L;
+    mix_layout(c, *spec, n_runs, threads, L);
+    if (!workspace || !c.ok()) return NZ_ERR_WORKSPACE;
+    L.m.key_ptr = key_dev;
+    L.m.n_runs = n_runs;
+    L.m.chain_share = spec->chain_share;
+    L.m.grid_min = spec->grid_min;
+    L.m.grid_max = spec->grid_max;
+    L.m.chain_min = spec->chain_min;
+    L.m.chain_max = spec->chain_max;
+    L.m.n_grid = spec->grid_max - spec->grid_min + 1;
+    L.m.n_chain = spec->chain_max - spec->chain_min + 1;
+    L.m.thr_grid = thr_grid;
+    L.m.thr_chain = thr_chain;
+    L.m.F = spec->checkpoints;
+    L.T = threads;
+    L.block = block;
+    L.smem_words = smem_words;
+    L.acc.count = out->count;
+    L.acc.span = out->span;
+    L.acc.sum_lo = out->sum_lo;
+    L.acc.sum_hi = out->sum_hi;
+    L.acc.m2 = out->m2;
+    L.acc.errors = out->errors;
+    ProfScope prof(NZ_PROF_UNION_FIND, as_stream(stream));
+    return launch_mix(L, as_stream(stream));
 }
 
 }  // extern "C"

@@ -767,7 +767,7 @@ void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, 
 // divided by N as microcanonical_averages_arrays returns them.
 // out[n * 21 + ...]: span (mean, lo, hi), max (mean, lo, hi), m0..m4 (mean, lo, hi).
 __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
-                                      double *out) {
+                                      int32_t normalize, double *out) {
     const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n > M) return;
     const double R = (double)*acc.count;
@@ -793,15 +793,16 @@ __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, 
             lo = mean + sc * student_t_quantile((1.0 - conf) / 2.0, R - 1.0);
             hi = mean + sc * student_t_quantile((1.0 + conf) / 2.0, R - 1.0);
         }
-        o[3 + 3 * j] = mean / N;
-        o[4 + 3 * j] = lo / N;
-        o[5 + 3 * j] = hi / N;
+        const double scale = normalize ? (double)N : 1.0;
+        o[3 + 3 * j] = mean / scale;
+        o[4 + 3 * j] = lo / scale;
+        o[5 + 3 * j] = hi / scale;
     }
 }
 
 void launch_micro_finalize(const NzMicroAccum &acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
-                           double *out, cudaStream_t s) {
-    micro_finalize_kernel<<<(M + 1 + 127) / 128, 128, 0, s>>>(acc, N, M, spanning, alpha, out);
+                           int32_t normalize, double *out, cudaStream_t s) {
+    micro_finalize_kernel<<<(M + 1 + 127) / 128, 128, 0, s>>>(acc, N, M, spanning, alpha, normalize, out);
 }
 
 __global__ void t_quantile_kernel(const double *q, const double *df, int32_t count, double *out) {

@@ -30,6 +30,8 @@ void launch_philox_perms(uint32_t M, int32_t n_runs, uint64_t key, uint64_t run0
                          cudaStream_t s);
 void launch_mt_perms(uint32_t M, int32_t n_runs, const uint32_t *seed_words, const int32_t *seed_len,
                      int32_t stride, uint32_t *out, cudaStream_t s);
+void launch_mt_stream_perms(const uint32_t *state_in, uint32_t M, int32_t n_runs, uint32_t *out,
+                            uint32_t *state_out, cudaStream_t s);
 void launch_pack_rows(const NzRecords &rec, int32_t run, uint32_t N, uint32_t M, int32_t spanning,
                       uint8_t *rows, cudaStream_t s);
 
@@ -77,7 +79,44 @@ void launch_bond_reduce(const uint8_t *a, const uint8_t *b, int32_t P, int32_t s
 void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, const double *ps,
                      double alpha, uint8_t *out, cudaStream_t s);
 void launch_micro_finalize(const NzMicroAccum &acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
-                           double *out, cudaStream_t s);
+                           int32_t normalize, double *out, cudaStream_t s);
 void launch_t_quantile(const double *q, const double *df, int32_t count, double *out, cudaStream_t s);
+
+// nz_mix.cu (batched uneven ensembles)
+struct MixDev {
+    const uint64_t *key_ptr;
+    int32_t n_runs;
+    uint32_t chain_share;
+    uint32_t grid_min, grid_max, chain_min, chain_max;
+    uint32_t n_grid, n_chain;
+    const uint32_t *thr_grid;
+    const uint32_t *thr_chain;
+    int32_t F;
+};
+struct MixRec {
+    uint32_t *max_span;
+    uint32_t *m0;
+    uint64_t *m2, *m3, *m4_lo;
+    uint32_t *m4_hi;
+};
+struct MixAccum {
+    uint32_t *count;
+    uint32_t *span;
+    uint64_t *sum_lo;
+    uint64_t *sum_hi;
+    double *m2;
+    uint32_t *errors;
+};
+struct MixLaunch {
+    MixDev m;
+    uint32_t *cls, *counts, *order, *offsets, *cursor, *queue, *head;
+    uint64_t *slot_off;
+    uint32_t *nodes;
+    int32_t T, block;
+    uint32_t smem_words;
+    MixRec rec;
+    MixAccum acc;
+};
+int launch_mix(const MixLaunch &p, cudaStream_t s);
 
 }  // namespace nz

@@ -1,0 +1,420 @@
+// nz_mix.cu -- batched uneven ensembles in one persistent launch.
+//
+// n_runs independent runs whose substrate is drawn per run: with probability
+// chain_share a spanning_1d_chain(l), l log-uniform in [chain_min, chain_max],
+// otherwise a spanning_2d_grid(L), L log-uniform in [grid_min, grid_max]
+// (percolate/percolate.py:899-965).  The draw and the bond permutation of
+// run r both come from Philox-4x32-10 keyed by `key` at counter r.
+//
+// Pipeline (all on the caller's stream, no host synchronisation):
+//   1. mix_class_kernel   : class of every run (threshold tables, no libm),
+//                           histogram of classes;
+//   2. mix_offsets_kernel : classes ordered by node count N descending
+//                           (longest-first scheduling) -> segment offsets;
+//   3. mix_scatter_kernel : run ids bucketed into a queue sorted by N desc;
+//   4. mix_slots_kernel   : node-slot offsets of the T persistent threads;
+//   5. mix_uf_kernel      : persistent union-find.  Thread t runs queue[t]
+//      first (its node slot is sized for it), then claims further items with
+//      an atomic counter; node counts only decrease along the queue, so every
+//      later item fits the slot.  Small items (4N <= smem slot) run in shared
+//      memory.  Each run writes its exact statistics at F evenly spaced
+//      occupation checkpoints n_j = floor(j M / (F - 1)).
+//   6. mix_reduce_kernel  : per (class, checkpoint) exact integer sums of x
+//      and x^2 (up to 192 bits) over the runs of the class -> mean and M2
+//      (percolate/percolate.py:450-705 semantics at those n).
+#include <cmath>
+#include <cstdint>
+
+#include "nz_common.cuh"
+#include "nz_internal.cuh"
+
+namespace nz {
+
+typedef unsigned __int128 u128;
+constexpr uint32_t kSizeTag = 0x53495A45u;  // "SIZE"
+
+
+__device__ __forceinline__ uint32_t class_of_run(const MixDev &m, uint64_t key, uint64_t r) {
+    uint32_t c[4] = {(uint32_t)r, (uint32_t)(r >> 32), 0u, kSizeTag};
+    philox4x32_10(c, (uint32_t)key, (uint32_t)(key >> 32));
+    const bool chain = c[0] < m.chain_share;
+    const uint32_t *thr = chain ? m.thr_chain : m.thr_grid;
+    const uint32_t n = chain ? m.n_chain : m.n_grid;
+    // largest i with thr[i] <= u (thr[0] == 0)
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (thr[mid] <= c[1]) lo = mid; else hi = mid;
+    }
+    return chain ? m.n_grid + lo : lo;
+}
+
+__device__ __forceinline__ void class_graph(const MixDev &m, uint32_t cls, uint32_t &kind, uint32_t &L,
+                                            uint32_t &N, uint32_t &M) {
+    if (cls < m.n_grid) {
+        kind = NZ_GRAPH_GRID2D; L = m.grid_min + cls; N = L * L; M = 2u * L * (L - 1u);
+    } else {
+        kind = NZ_GRAPH_CHAIN1D; L = m.chain_min + (cls - m.n_grid); N = L; M = L - 1u;
+    }
+}
+
+__global__ void mix_class_kernel(MixDev m, uint32_t *cls, uint32_t *counts) {
+    const uint64_t key = *m.key_ptr;
+    for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m.n_runs; r += gridDim.x * blockDim.x) {
+        const uint32_t c = class_of_run(m, key, (uint64_t)r);
+        cls[r] = c;
+        atomicAdd(&counts[c], 1u);
+    }
+}
+
+// Position of every class in the order "node count N descending, grids
+// before chains on equal N" (grid N = L^2 and chain N = l both increase with
+// the length).  Ordering by N -- not by M -- is what makes the persistent
+// threads' node slots safe: every item after position t has at most the
+// nodes of item t.
+__global__ void mix_order_kernel(MixDev m, uint32_t *order) {
+    const uint32_t n_classes = m.n_grid + m.n_chain;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n_classes; c += gridDim.x * blockDim.x) {
+        uint32_t rank;
+        if (c < m.n_grid) {
+            const uint64_t Nc = (uint64_t)(m.grid_min + c) * (m.grid_min + c);
+            // chains with more nodes: l >= Nc + 1
+            const uint64_t lo = Nc + 1u;
+            const uint32_t more = lo > m.chain_max ? 0u
+                                : (uint32_t)(m.chain_max - (lo > m.chain_min ? lo : (uint64_t)m.chain_min) + 1u);
+            rank = (m.n_grid - 1u - c) + more;
+        } else {
+            const uint32_t k = c - m.n_grid;
+            const uint64_t Nk = (uint64_t)m.chain_min + k;
+            // grids with at least as many nodes: smallest L in range with L^2 >= Nk
+            uint32_t a = m.grid_min, b = m.grid_max + 1u;
+            while (a < b) {
+                const uint32_t mid = (a + b) >> 1;
+                if ((uint64_t)mid * mid >= Nk) b = mid; else a = mid + 1u;
+            }
+            rank = (m.n_chain - 1u - k) + (m.grid_max + 1u - a);
+        }
+        order[rank] = c;
+    }
+}
+
+__global__ void mix_head_kernel(uint32_t *head, uint32_t v) { *head = v; }
+
+// Single block: exclusive scan of counts taken in the order `order` (classes
+// by N descending) -> offsets[c]; also the cursor copy used by the scatter.
+__global__ void mix_offsets_kernel(const uint32_t *counts, const uint32_t *order, uint32_t n_classes,
+                                   uint32_t *offsets, uint32_t *cursor) {
+    __shared__ uint32_t s[1024];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n_classes; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t v = i < n_classes ? counts[order[i]] : 0u;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            const uint32_t y = threadIdx.x >= (unsigned)off ? s[threadIdx.x - off] : 0u;
+            __syncthreads();
+            s[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (i < n_classes) {
+            const uint32_t ex = carry + s[threadIdx.x] - v;
+            offsets[order[i]] = ex;
+            cursor[order[i]] = ex;
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += s[1023];
+        __syncthreads();
+    }
+}
+
+__global__ void mix_scatter_kernel(int32_t n_runs, const uint32_t *cls, uint32_t *cursor, uint32_t *queue) {
+    for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_runs; r += gridDim.x * blockDim.x)
+        queue[atomicAdd(&cursor[cls[r]], 1u)] = (uint32_t)r;
+}
+
+// Node-slot offsets (in words) of the T persistent threads: exclusive scan of
+// N(queue[t]) for t < T (single block).
+__global__ void mix_slots_kernel(MixDev m, const uint32_t *queue, const uint32_t *cls, int32_t T,
+                                 uint64_t *slot_off) {
+    __shared__ uint64_t s[1024];
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int32_t base = 0; base < T; base += 1024) {
+        const int32_t t = base + threadIdx.x;
+        uint64_t v = 0;
+        if (t < T && t < m.n_runs) {
+            uint32_t kind, L, N, M;
+            class_graph(m, cls[queue[t]], kind, L, N, M);
+            v = N;
+        }
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            const uint64_t y = threadIdx.x >= (unsigned)off ? s[threadIdx.x - off] : 0ull;
+            __syncthreads();
+            s[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (t < T) slot_off[t] = carry + s[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += s[1023];
+        __syncthreads();
+        if (threadIdx.x == 0 && base + 1024 >= T) slot_off[T] = carry;
+    }
+}
+
+
+__device__ __forceinline__ void add128m(uint64_t &lo, uint64_t &hi, uint64_t blo, uint64_t bhi) {
+    const uint64_t nlo = lo + blo;
+    hi += bhi + (nlo < lo ? 1ull : 0ull);
+    lo = nlo;
+}
+
+// One complete run in `node` (global or shared), writing its checkpoints.
+template <int KIND>
+__device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L, uint32_t N, uint32_t M, uint32_t *node,
+                        const MixRec &out, size_t rec_base) {
+    GraphDev g;
+    g.kind = KIND; g.L = L; g.N = N; g.M = M;
+    g.two_l_m1 = KIND == NZ_GRAPH_GRID2D ? 2u * L - 1u : 1u;
+    g.row_edges = KIND == NZ_GRAPH_GRID2D ? (L - 1u) * g.two_l_m1 : 0u;
+    g.inv_two_l_m1 = 1.0f / (float)g.two_l_m1;
+    g.eu = g.ev = nullptr; g.side = nullptr;
+    for (uint32_t i = 0; i < N; ++i) node[i] = make_root(1u, node_sides<KIND>(g, i));
+    FeistelPerm fp;
+    fp.init(key, run, M);
+    uint64_t t2 = N, t3 = N, t4lo = N, t4hi = 0;
+    uint32_t t0 = N, mx = 1;
+    uint64_t mx2 = 1, mx3 = 1, mx4lo = 1, mx4hi = 0;
+    bool span = false;
+    const uint32_t Fm1 = (uint32_t)m.F - 1u;
+    uint32_t j = 0;
+    // checkpoint j is the row n_j = floor(j * M / (F - 1))
+    auto next_row = [&](uint32_t jj) -> uint32_t {
+        return (uint32_t)(((uint64_t)jj * M) / Fm1);
+    };
+    uint32_t target = next_row(0);
+    for (uint32_t n = 0; n <= M; ++n) {
+        if (n > 0) {
+            const uint32_t e = fp.at(n - 1u);
+            uint32_t u, v;
+            decode_edge<KIND>(g, e, u, v);
+            uint32_t xu = u, xv = v;
+            uint32_t wu = node[xu], wv = node[xv];
+            for (int hops = 0; !(is_root(wu) && is_root(wv)); ++hops) {
+                if (hops >= 64) { wu = wv = make_root(0, 0); xu = xv; break; }
+                if (!is_root(wu)) {
+                    const uint32_t nu = node[wu];
+                    if (!is_root(nu)) node[xu] = nu;
+                    xu = wu; wu = nu;
+                }
+                if (!is_root(wv)) {
+                    const uint32_t nv = node[wv];
+                    if (!is_root(nv)) node[xv] = nv;
+                    xv = wv; wv = nv;
+                }
+            }
+            if (xu != xv) {
+                const uint32_t a = root_size(wu), b = root_size(wv);
+                const uint32_t sides = root_sides(wu) | root_sides(wv);
+                const uint32_t s = a + b;
+                uint32_t big = xu, small = xv;
+                if (a < b) { big = xv; small = xu; }
+                node[small] = big;
+                node[big] = make_root(s, sides);
+                t0 -= 1u;
+                const uint64_t ab = (uint64_t)a * b;
+                t2 += 2ull * ab;
+                t3 += 3ull * ab * s;
+                const uint64_t q = 4ull * a * a + 6ull * ab + 4ull * b * b;
+                add128m(t4lo, t4hi, ab * q, __umul64hi(ab, q));
+                if (s > mx) {
+                    mx = s; mx2 = (uint64_t)mx * mx; mx3 = mx2 * mx;
+                    mx4lo = mx3 * mx; mx4hi = __umul64hi(mx3, (uint64_t)mx);
+                }
+                if (sides == 3u) span = true;
+            }
+        }
+        while (j < (uint32_t)m.F && n == target) {
+            const size_t off = rec_base + j;
+            out.max_span[off] = mx | (span ? kSpanBit : 0u);
+            out.m0[off] = t0 - 1u;
+            out.m2[off] = t2 - mx2;
+            out.m3[off] = t3 - mx3;
+            out.m4_lo[off] = t4lo - mx4lo;
+            out.m4_hi[off] = (uint32_t)(t4hi - mx4hi - (t4lo < mx4lo ? 1ull : 0ull));
+            ++j;
+            if (j < (uint32_t)m.F) target = next_row(j);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) mix_uf_kernel(MixDev m, const uint32_t *queue, const uint32_t *cls,
+                                                     int32_t T, const uint64_t *slot_off, uint32_t *nodes,
+                                                     uint32_t smem_words, uint32_t *head, MixRec out,
+                                                     uint32_t *errors) {
+    extern __shared__ uint32_t s_nodes[];
+    const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T || t >= m.n_runs) return;
+    const uint64_t key = *m.key_ptr;
+    uint32_t *gslot = nodes + slot_off[t];
+    const uint64_t slot_words = slot_off[t + 1] - slot_off[t];
+    uint32_t *sslot = smem_words ? s_nodes + (size_t)threadIdx.x * smem_words : nullptr;
+    uint32_t pos = (uint32_t)t;
+    while (pos < (uint32_t)m.n_runs) {
+        const uint32_t run = queue[pos];
+        uint32_t kind, L, N, M;
+        class_graph(m, cls[run], kind, L, N, M);
+        uint32_t *node = (sslot && N <= smem_words) ? sslot : gslot;
+        if (node == gslot && N > slot_words) {  // cannot happen with the N-descending queue
+            atomicAdd(errors, 1u);
+            pos = atomicAdd(head, 1u);
+            continue;
+        }
+        const size_t base = (size_t)pos * (uint32_t)m.F;
+        if (kind == NZ_GRAPH_GRID2D) mix_run<NZ_GRAPH_GRID2D>(m, key, run, L, N, M, node, out, base);
+        else mix_run<NZ_GRAPH_CHAIN1D>(m, key, run, L, N, M, node, out, base);
+        pos = atomicAdd(head, 1u);
+    }
+}
+
+// ---------------------------------------------------------------- reduction
+// Unsigned 256-bit helpers (4 little-endian 64-bit limbs).
+struct U256 { uint64_t w[4]; };
+
+__device__ __forceinline__ void u256_add(U256 &a, const U256 &b) {
+    uint64_t c = 0;
+    for (int i = 0; i < 4; ++i) {
+        const uint64_t s = a.w[i] + b.w[i];
+        const uint64_t c1 = s < a.w[i];
+        const uint64_t s2 = s + c;
+        const uint64_t c2 = s2 < s;
+        a.w[i] = s2;
+        c = c1 | c2;
+    }
+}
+__device__ __forceinline__ U256 u256_from_u128(u128 x) {
+    U256 r = {{(uint64_t)x, (uint64_t)(x >> 64), 0, 0}};
+    return r;
+}
+// a (< 2^128) squared
+__device__ __forceinline__ U256 u128_sq(u128 a) {
+    const uint64_t lo = (uint64_t)a, hi = (uint64_t)(a >> 64);
+    const u128 ll = (u128)lo * lo, lh = (u128)lo * hi, hh = (u128)hi * hi;
+    U256 r = u256_from_u128(ll);
+    U256 mid = {{0, (uint64_t)lh, (uint64_t)(lh >> 64), 0}};
+    u256_add(r, mid);
+    u256_add(r, mid);
+    U256 top = {{0, 0, (uint64_t)hh, (uint64_t)(hh >> 64)}};
+    u256_add(r, top);
+    return r;
+}
+// a * k for k < 2^64
+__device__ __forceinline__ U256 u256_mul64(const U256 &a, uint64_t k) {
+    U256 r = {{0, 0, 0, 0}};
+    u128 carry = 0;
+    for (int i = 0; i < 4; ++i) {
+        const u128 p = (u128)a.w[i] * k + carry;
+        r.w[i] = (uint64_t)p;
+        carry = p >> 64;
+    }
+    return r;
+}
+// a - b (a >= b)
+__device__ __forceinline__ U256 u256_sub(const U256 &a, const U256 &b) {
+    U256 r;
+    uint64_t borrow = 0;
+    for (int i = 0; i < 4; ++i) {
+        const uint64_t d = a.w[i] - b.w[i];
+        const uint64_t b1 = a.w[i] < b.w[i];
+        const uint64_t d2 = d - borrow;
+        const uint64_t b2 = d < borrow;
+        r.w[i] = d2;
+        borrow = b1 | b2;
+    }
+    return r;
+}
+__device__ __forceinline__ double u256_to_f64(const U256 &a) {
+    const double t64 = 18446744073709551616.0;
+    return ((a.w[3] * t64 + (double)a.w[2]) * t64 + (double)a.w[1]) * t64 + (double)a.w[0];
+}
+__device__ __forceinline__ double u128_f64(u128 x) {
+    return fma((double)(uint64_t)(x >> 64), 18446744073709551616.0, (double)(uint64_t)x);
+}
+
+
+// grid (classes, ceil(F / 32)); thread = checkpoint j; loop over the class's runs.
+__global__ void mix_reduce_kernel(MixDev m, const uint32_t *counts, const uint32_t *offsets, MixRec rec,
+                                  MixAccum acc, uint32_t n_classes) {
+    const uint32_t c = blockIdx.x;
+    const uint32_t j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (c >= n_classes || j >= (uint32_t)m.F) return;
+    const uint32_t cnt = counts[c], off = offsets[c];
+    uint32_t kind, L, N, M;
+    class_graph(m, c, kind, L, N, M);
+    (void)kind; (void)L; (void)M;
+    uint32_t span = 0;
+    u128 sx[6] = {0, 0, 0, 0, 0, 0};
+    U256 sq[6];
+    for (int k = 0; k < 6; ++k) sq[k] = U256{{0, 0, 0, 0}};
+    for (uint32_t i = 0; i < cnt; ++i) {
+        const size_t o = (size_t)(off + i) * (uint32_t)m.F + j;
+        const uint32_t ms = rec.max_span[o];
+        const uint32_t mxv = ms & ~kSpanBit;
+        span += ms >> 31;
+        const u128 x[6] = {mxv, rec.m0[o], (u128)(N - mxv), rec.m2[o], rec.m3[o],
+                           ((u128)rec.m4_hi[o] << 64) | rec.m4_lo[o]};
+        for (int k = 0; k < 6; ++k) {
+            sx[k] += x[k];
+            u256_add(sq[k], u128_sq(x[k]));
+        }
+    }
+    const size_t cj = (size_t)c * (uint32_t)m.F + j;
+    const size_t plane = (size_t)n_classes * (uint32_t)m.F;
+    if (j == 0) acc.count[c] = cnt;
+    acc.span[cj] = span;
+    for (int k = 0; k < 6; ++k) {
+        acc.sum_lo[k * plane + cj] = (uint64_t)sx[k];
+        acc.sum_hi[k * plane + cj] = (uint64_t)(sx[k] >> 64);
+        // M2 = (cnt * sum x^2 - (sum x)^2) / cnt, numerator exact in 256 bits
+        double m2 = 0.0;
+        if (cnt > 0) {
+            const U256 num = u256_sub(u256_mul64(sq[k], cnt), u128_sq(sx[k]));
+            m2 = u256_to_f64(num) / (double)cnt;
+        }
+        acc.m2[k * plane + cj] = m2;
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+int launch_mix(const MixLaunch &p, cudaStream_t s) {
+    const uint32_t n_classes = p.m.n_grid + p.m.n_chain;
+    if (cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * n_classes, s) != cudaSuccess) return NZ_ERR_CUDA;
+    if (cudaMemsetAsync(p.acc.errors, 0, sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
+    int blocks = (p.m.n_runs + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    mix_class_kernel<<<blocks, 256, 0, s>>>(p.m, p.cls, p.counts);
+    mix_order_kernel<<<(n_classes + 255) / 256, 256, 0, s>>>(p.m, p.order);
+    mix_offsets_kernel<<<1, 1024, 0, s>>>(p.counts, p.order, n_classes, p.offsets, p.cursor);
+    mix_scatter_kernel<<<blocks, 256, 0, s>>>(p.m.n_runs, p.cls, p.cursor, p.queue);
+    mix_slots_kernel<<<1, 1024, 0, s>>>(p.m, p.queue, p.cls, p.T, p.slot_off);
+    const uint32_t first_free = (uint32_t)(p.T < p.m.n_runs ? p.T : p.m.n_runs);
+    mix_head_kernel<<<1, 1, 0, s>>>(p.head, first_free);
+    const size_t smem = (size_t)p.smem_words * 4u * (size_t)p.block;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(mix_uf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return NZ_ERR_INVALID;
+    mix_uf_kernel<<<(p.T + p.block - 1) / p.block, p.block, smem, s>>>(p.m, p.queue, p.cls, p.T, p.slot_off,
+                                                                        p.nodes, p.smem_words, p.head, p.rec,
+                                                                        p.acc.errors);
+    dim3 rg(n_classes, (p.m.F + 31) / 32);
+    mix_reduce_kernel<<<rg, 32, 0, s>>>(p.m, p.counts, p.offsets, p.rec, p.acc, n_classes);
+    return cudaGetLastError() == cudaSuccess ? NZ_OK : NZ_ERR_CUDA;
+}
+
+}  // namespace nz

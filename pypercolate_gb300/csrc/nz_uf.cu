@@ -228,6 +228,37 @@ __global__ void mt_perm_kernel(uint32_t M, int32_t n_runs, const uint32_t *seed_
     }
 }
 
+// Continuation of one MT19937 stream (numpy's global RandomState): the state
+// (624 words + position) is loaded, n_runs permutations of range(M) are drawn
+// one after another exactly as np.random.permutation(M) would draw them
+// (percolate/percolate.py:270, once per run in run order), and the advanced
+// state is stored back.  One thread: the stream is sequential by nature.
+__global__ void mt_stream_perm_kernel(const uint32_t *state_in, uint32_t M, int32_t n_runs, uint32_t *out,
+                                      uint32_t *state_out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    Mt19937 g;
+    for (int i = 0; i < 624; ++i) g.mt[i] = state_in[i];
+    g.mti = (int)state_in[624];
+    for (int32_t r = 0; r < n_runs; ++r) {
+        uint32_t *o = out + (size_t)r * M;
+        for (uint32_t i = 0; i < M; ++i) o[i] = i;
+        for (int64_t i = (int64_t)M - 1; i >= 1; --i) {
+            uint32_t mx = (uint32_t)i, mask = mx;
+            mask |= mask >> 1; mask |= mask >> 2; mask |= mask >> 4; mask |= mask >> 8; mask |= mask >> 16;
+            uint32_t j;
+            do { j = g.next() & mask; } while (j > mx);
+            uint32_t t = o[i]; o[i] = o[j]; o[j] = t;
+        }
+    }
+    for (int i = 0; i < 624; ++i) state_out[i] = g.mt[i];
+    state_out[624] = (uint32_t)g.mti;
+}
+
+void launch_mt_stream_perms(const uint32_t *state_in, uint32_t M, int32_t n_runs, uint32_t *out,
+                            uint32_t *state_out, cudaStream_t s) {
+    mt_stream_perm_kernel<<<1, 1, 0, s>>>(state_in, M, n_runs, out, state_out);
+}
+
 // ---------------------------------------------------------------- packing
 // Reference row layout (packed little-endian), percolate/hpc.py:34-70:
 //   n u32 | edge u32 | [has_spanning_cluster u8] | max_cluster_size u32 | moments 5 x u64

@@ -123,8 +123,8 @@ class Ensemble:
         torch = nat.torch_cuda()
         out = torch.empty((self.M + 1) * 21, dtype=torch.float64, device='cuda')
         st = nat.lib_handle().nz_microcanonical_finalize(
-            self._micro_struct(), self.N, self.M, int(self.spanning), float(alpha), nat.ptr(out),
-            nat.stream_handle())
+            self._micro_struct(), self.N, self.M, int(self.spanning), float(alpha), 1,
+            nat.ptr(out), nat.stream_handle())
         nat.check(st, 'nz_microcanonical_finalize')
         o = out.cpu().numpy().reshape(self.M + 1, 21)
         ret = {'N': self.N, 'M': self.M}

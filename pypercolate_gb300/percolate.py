@@ -201,3 +201,241 @@ def binomial_pmfs(n, ps):
     nat.check(nat.lib_handle().nz_binomial_pmf(n, nat.ptr(dps), len(ps), nat.ptr(out),
                                                nat.stream_handle()), 'nz_binomial_pmf')
     return out.cpu().numpy().reshape(len(ps), n + 1)
+
+
+# ---------------------------------------------------------------------------
+# classic microcanonical / canonical API (percolate/percolate.py:708-1252)
+# ---------------------------------------------------------------------------
+_MICRO_RECORD_BUDGET = 1 << 30  # bytes of per-step records per launch
+
+
+def _micro_accumulators(rows):
+    torch = nat.torch_cuda()
+    acc = dict(count=torch.zeros(1, dtype=torch.int64, device='cuda'),
+               span_count=torch.zeros(rows, dtype=torch.int64, device='cuda'),
+               sum_lo=torch.zeros(6 * rows, dtype=torch.int64, device='cuda'),
+               sum_hi=torch.zeros(6 * rows, dtype=torch.int64, device='cuda'),
+               m2=torch.zeros(6 * rows, dtype=torch.float64, device='cuda'))
+    s = nat.NzMicroAccum()
+    for k, v in acc.items():
+        setattr(s, k, v.data_ptr())
+    return acc, s
+
+
+def _finalize_micro(acc_struct, N, M, spanning, alpha, normalize):
+    torch = nat.torch_cuda()
+    out = torch.empty((M + 1) * 21, dtype=torch.float64, device='cuda')
+    nat.check(nat.lib_handle().nz_microcanonical_finalize(
+        acc_struct, N, M, int(spanning), float(alpha), int(normalize), nat.ptr(out),
+        nat.stream_handle()), 'nz_microcanonical_finalize')
+    return out.cpu().numpy().reshape(M + 1, 21)
+
+
+def _global_stream_perms(M, runs):
+    """The next `runs` permutations np.random.permutation(M) would return
+    (drawn on the GPU from numpy's global MT19937 state, which is advanced
+    exactly as the draws would advance it)."""
+    torch = nat.torch_cuda()
+    name, keys, pos, has_gauss, gauss = np.random.get_state()
+    if name != 'MT19937':
+        raise ValueError('numpy global RandomState is not MT19937')
+    state = np.empty(625, dtype=np.uint32)
+    state[:624] = keys
+    state[624] = pos
+    d_in = torch.from_numpy(state.view(np.int32).copy()).cuda()
+    d_out = torch.empty(625, dtype=torch.int32, device='cuda')
+    perms = torch.empty(max(runs * M, 1), dtype=torch.int32, device='cuda')
+    nat.check(nat.lib_handle().nz_mt_stream_permutations(
+        nat.ptr(d_in), int(M), int(runs), nat.ptr(perms), nat.ptr(d_out), nat.stream_handle()),
+        'nz_mt_stream_permutations')
+    new = d_out.cpu().numpy().view(np.uint32)
+    np.random.set_state((name, new[:624].copy(), int(new[624]), has_gauss, gauss))
+    return perms
+
+
+class _MicroAverages:
+    """Iterator of percolate.microcanonical_averages (see that function)."""
+
+    def __init__(self, graph, runs, spanning_cluster, model, alpha, copy_result):
+        self._args = (graph, runs, spanning_cluster, model, alpha)
+        self._copy = copy_result
+        self._n = 0
+        self._rows = None
+        self._ret = {}
+
+    def __iter__(self):
+        return self
+
+    def _validate(self):
+        graph, runs, spanning_cluster, model, alpha = self._args
+        try:
+            runs = int(runs)
+        except (TypeError, ValueError):
+            raise ValueError('runs needs to be a positive integer')
+        if runs <= 0:
+            raise ValueError('runs needs to be a positive integer')
+        try:
+            alpha = float(alpha)
+        except (TypeError, ValueError):
+            raise ValueError('alpha needs to be a float in the interval (0, 1)')
+        if alpha <= 0.0 or alpha >= 1.0:
+            raise ValueError('alpha needs to be a float in the interval (0, 1)')
+        if model != 'bond':
+            raise ValueError('Only bond percolation supported.')
+        pg = percolation_graph(graph, spanning_cluster=spanning_cluster)
+        from . import hpc
+        self._spec = hpc.graph_spec(**pg)
+        self._runs, self._alpha, self._spanning = runs, alpha, bool(spanning_cluster)
+
+    def _initial_row(self):
+        """n = 0 for every run: no permutation is drawn yet (as in the
+        reference, whose runs draw theirs at their second step)."""
+        torch = nat.torch_cuda()
+        N, R = self._spec.N, self._runs
+        acc, s = _micro_accumulators(1)
+        acc['count'].fill_(R)
+        # max = 1, and every moment (m1 = N - max included) is N - 1
+        vals = torch.tensor([1, N - 1, N - 1, N - 1, N - 1, N - 1], dtype=torch.int64,
+                            device='cuda') * R
+        acc['sum_lo'].copy_(vals)
+        return _finalize_micro(s, N, 0, self._spanning, self._alpha, 0)[0]
+
+    def _all_rows(self, normalize=0):
+        from . import hpc
+        spec, R = self._spec, self._runs
+        N, M = spec.N, spec.M
+        perms = _global_stream_perms(M, R)
+        acc, s = _micro_accumulators(M + 1)
+        chunk = max(1, min(R, _MICRO_RECORD_BUDGET // (36 * (M + 1))))
+        for r0 in range(0, R, chunk):
+            rc = min(chunk, R - r0)
+            p = perms[r0 * M:(r0 + rc) * M].cpu().numpy().view(np.uint32).reshape(rc, M)
+            rec = hpc._run_microcanonical(spec, self._spanning, perms=p if M else None,
+                                          seeds=None if M else [0] * rc, with_edge=False)
+            nat.check(nat.lib_handle().nz_microcanonical_reduce(
+                rec.struct(), N, M, rc, 0, M + 1, s, nat.stream_handle()),
+                'nz_microcanonical_reduce')
+        return _finalize_micro(s, N, M, self._spanning, self._alpha, normalize)
+
+    def _row_dict(self, n, o):
+        spec = self._spec
+        ret = dict() if self._copy else self._ret
+        ret['n'] = n
+        ret['N'] = spec.N
+        ret['M'] = spec.M
+        ret['max_cluster_size'] = float(o[3])
+        ret['max_cluster_size_ci'] = np.array(o[4:6])
+        ret['moments'] = np.array(o[6:21:3])
+        ret['moments_ci'] = np.stack([o[7 + 3 * k:9 + 3 * k] for k in range(5)])
+        if self._spanning:
+            ret['spanning_cluster'] = float(o[0])
+            ret['spanning_cluster_ci'] = np.array(o[1:3])
+        return ret
+
+    def __next__(self):
+        if self._n == 0:
+            self._validate()
+            row = self._initial_row()
+        else:
+            if self._n > self._spec.M:
+                raise StopIteration
+            if self._rows is None:
+                self._rows = self._all_rows()
+            row = self._rows[self._n]
+        out = self._row_dict(self._n, row)
+        self._n += 1
+        return out
+
+    def arrays(self):
+        """microcanonical_averages_arrays of a fresh iterator, normalised on the GPU."""
+        if self._n != 0:
+            raise ValueError('iterator already advanced')
+        self._validate()
+        self._n = self._spec.M + 1
+        o = self._all_rows(normalize=1)
+        ret = {'N': self._spec.N, 'M': self._spec.M}
+        ret['max_cluster_size'] = o[:, 3].copy()
+        ret['max_cluster_size_ci'] = o[:, 4:6].copy()
+        if self._spanning:
+            ret['spanning_cluster'] = o[:, 0].copy()
+            ret['spanning_cluster_ci'] = o[:, 1:3].copy()
+        ret['moments'] = np.stack([o[:, 6 + 3 * k] for k in range(5)])
+        ret['moments_ci'] = np.stack([o[:, 7 + 3 * k:9 + 3 * k] for k in range(5)])
+        return ret
+
+
+def microcanonical_averages(graph, runs=40, spanning_cluster=True, model='bond',
+                            alpha=alpha_1sigma, copy_result=True):
+    """Microcanonical ensemble averages over `runs` runs for n = 0..M
+    (percolate/percolate.py:708-896).  Yields one dict per n (absolute units,
+    like the reference).  The runs draw np.random.permutation(M) in turn from
+    numpy's global RandomState (continued on the GPU), so a given
+    np.random.seed reproduces the reference's averages; the whole ensemble is
+    computed by the union-find and run-reduction kernels when n = 1 is
+    requested.  ValueErrors are raised at the first next()."""
+    return _MicroAverages(graph, runs, spanning_cluster, model, alpha, copy_result)
+
+
+def microcanonical_averages_arrays(microcanonical_averages):
+    """Arrays over n of the microcanonical averages, max and moments divided
+    by N (percolate/percolate.py:968-1064)."""
+    if isinstance(microcanonical_averages, _MicroAverages):
+        return microcanonical_averages.arrays()
+    ret = dict()
+    for n, avg in enumerate(microcanonical_averages):
+        assert n == avg['n']
+        if n == 0:
+            M, N = avg['M'], avg['N']
+            spanning = 'spanning_cluster' in avg
+            ret['max_cluster_size'] = np.empty(M + 1)
+            ret['max_cluster_size_ci'] = np.empty((M + 1, 2))
+            if spanning:
+                ret['spanning_cluster'] = np.empty(M + 1)
+                ret['spanning_cluster_ci'] = np.empty((M + 1, 2))
+            ret['moments'] = np.empty((5, M + 1))
+            ret['moments_ci'] = np.empty((5, M + 1, 2))
+        ret['max_cluster_size'][n] = avg['max_cluster_size']
+        ret['max_cluster_size_ci'][n] = avg['max_cluster_size_ci']
+        if spanning:
+            ret['spanning_cluster'][n] = avg['spanning_cluster']
+            ret['spanning_cluster_ci'][n] = avg['spanning_cluster_ci']
+        ret['moments'][:, n] = avg['moments']
+        ret['moments_ci'][:, n] = avg['moments_ci']
+    for key in list(ret):
+        if 'spanning_cluster' not in key:
+            ret[key] = ret[key] / N
+    ret['M'], ret['N'] = M, N
+    return ret
+
+
+def canonical_averages(ps, microcanonical_averages_arrays):
+    """Canonical averages at each p: binomial weights (FP64, GPU) times every
+    microcanonical array, confidence bounds included, as the reference does
+    (percolate/percolate.py:1112-1221); one FP64 GEMM on the GPU."""
+    torch = nat.torch_cuda()
+    arr = microcanonical_averages_arrays
+    N, M = arr['N'], arr['M']
+    ps = np.asarray(ps, dtype=np.float64)
+    spanning = 'spanning_cluster' in arr
+    cols = [arr['max_cluster_size'][:, None], arr['max_cluster_size_ci'],
+            arr['moments'].T, arr['moments_ci'].transpose(1, 0, 2).reshape(M + 1, 10)]
+    if spanning:
+        cols += [arr['spanning_cluster'][:, None], arr['spanning_cluster_ci']]
+    V = torch.from_numpy(np.ascontiguousarray(np.hstack(cols))).cuda()
+    W = torch.from_numpy(binomial_pmfs(M, ps.ravel())).cuda()
+    C = (W @ V).cpu().numpy()
+    ret = {'ps': ps, 'N': N, 'M': M}
+    ret['max_cluster_size'] = C[:, 0]
+    ret['max_cluster_size_ci'] = C[:, 1:3]
+    ret['moments'] = C[:, 3:8].T.copy()
+    ret['moments_ci'] = C[:, 8:18].reshape(-1, 5, 2).transpose(1, 0, 2).copy()
+    if spanning:
+        ret['spanning_cluster'] = C[:, 18]
+        ret['spanning_cluster_ci'] = C[:, 19:21]
+    return ret
+
+
+def statistics(graph, ps, spanning_cluster=True, model='bond', alpha=alpha_1sigma, runs=40):
+    """Canonical statistics of `graph` (percolate/percolate.py:1226-1252)."""
+    return canonical_averages(ps, microcanonical_averages_arrays(microcanonical_averages(
+        graph=graph, runs=runs, spanning_cluster=spanning_cluster, model=model, alpha=alpha)))

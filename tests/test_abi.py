@@ -122,3 +122,18 @@ def test_graph_spec_side_masks():
     # non-spanning on the same graph falls back to the explicit (L+2) x L grid
     spec = hpc.graph_spec(**percolation_graph(P.spanning_2d_grid(4), spanning_cluster=False))
     assert spec.kind == 2 and spec.N == 24
+
+
+def test_log_uniform_thresholds():
+    from pypercolate_gb300.mix import log_uniform_thresholds
+    thr = log_uniform_thresholds(8, 512)
+    assert thr[0] == 0 and len(thr) == 505
+    assert np.all(np.diff(thr.astype(np.int64)) >= 0)
+    rng = np.random.default_rng(0)
+    u = rng.integers(0, 2 ** 32, size=400000, dtype=np.uint64)
+    L = 8 + np.searchsorted(thr.astype(np.uint64), u, side='right') - 1
+    assert L.min() == 8 and L.max() == 512
+    # log-uniform: median at sqrt(8 * 512) = 64, quartiles at 22.6 and 181
+    assert abs(np.mean(L <= 64) - 0.5) < 0.01
+    assert abs(np.mean(L <= 22) - 0.25) < 0.02
+    assert np.array_equal(log_uniform_thresholds(5, 5), [0])

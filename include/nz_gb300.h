@@ -305,6 +305,37 @@ int nz_mix(const NzMixSpec *spec, const uint32_t *thr_grid,
            void *workspace, size_t workspace_bytes, const NzMixAccum *out,
            void *stream);
 
+/* ---- MLP surrogate of the canonical curves ---------------------------- */
+/* (No counterpart in the reference.)  Fully connected, GELU hidden layers,
+ * linear output; widths[0..n_layers] (host array).  GEMM operands are
+ * BF16 (activations and gradients rounded to nearest-even where they enter
+ * a product), accumulation FP32.  params: flat FP32, per layer W [in][out]
+ * row-major then b [out]; params_bf16: its BF16 mirror (2 bytes each). */
+int64_t nz_mlp_param_count(const int32_t *widths, int32_t n_layers);
+/* floats of z (pre-activations) and of h (activations) for a batch */
+int64_t nz_mlp_activation_count(const int32_t *widths, int32_t n_layers,
+                                int32_t batch);
+int nz_mlp_params_to_bf16(const float *params, int64_t count,
+                          void *params_bf16, void *stream);
+int nz_mlp_forward(const int32_t *widths, int32_t n_layers, int32_t batch,
+                   const float *x, const float *params,
+                   const void *params_bf16, float *z, float *h, float *y,
+                   void *stream);
+/* weighted squared error over [batch][n_out]: loss_parts[i] partial sums of
+ * sum w (y - t)^2 / batch (add them up), dy = 2 w (y - t) / batch */
+int nz_mlp_loss(const float *y, const float *target, const float *weight,
+                int32_t batch, int32_t n_out, float *dy, float *loss_parts,
+                int32_t n_parts, void *stream);
+/* scratch: 2 * batch * max(widths) floats */
+int nz_mlp_backward(const int32_t *widths, int32_t n_layers, int32_t batch,
+                    const float *x, const void *params_bf16, const float *z,
+                    const float *h, const float *dy, float *grads,
+                    float *scratch, void *stream);
+/* Adam step (step >= 1); also refreshes params_bf16 */
+int nz_mlp_adam(float *params, const float *grads, float *m, float *v,
+                void *params_bf16, int64_t count, float lr, float beta1,
+                float beta2, float eps, int32_t step, void *stream);
+
 /* ---- memory-system hint ------------------------------------------------ */
 /* L2 fetch granularity of the calling CUDA context (cudaLimitMaxL2FetchGranularity:
  * 0, 32, 64 or 128 bytes).  The union-find reads scattered 4-byte node words;

@@ -118,6 +118,18 @@ _SIGNATURES = [
     ('nz_mix', ctypes.c_int,
      [ctypes.POINTER(NzMixSpec), _vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32,
       ctypes.c_int32, ctypes.c_uint32, _vp, ctypes.c_size_t, ctypes.POINTER(NzMixAccum), _vp]),
+    ('nz_mlp_param_count', ctypes.c_int64, [_vp, ctypes.c_int32]),
+    ('nz_mlp_activation_count', ctypes.c_int64, [_vp, ctypes.c_int32, ctypes.c_int32]),
+    ('nz_mlp_params_to_bf16', ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp]),
+    ('nz_mlp_forward', ctypes.c_int,
+     [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ('nz_mlp_loss', ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp]),
+    ('nz_mlp_backward', ctypes.c_int,
+     [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ('nz_mlp_adam', ctypes.c_int,
+     [_vp, _vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+      ctypes.c_float, ctypes.c_int32, _vp]),
     ('nz_set_l2_fetch_granularity', ctypes.c_int, [ctypes.c_int32]),
     ('nz_get_l2_fetch_granularity', ctypes.c_int, [_vp]),
     ('nz_profile_enable', None, [ctypes.c_int32]),

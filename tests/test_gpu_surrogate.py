@@ -1,0 +1,95 @@
+"""MLP surrogate: forward/backward kernels against the FP64 CPU oracle,
+training, the Monte Carlo acceptance rule, and what the surrogate gains when
+it places the p-grid of a held-out lattice size."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from pypercolate_gb300 import _native as nat
+    nat.lib_handle()
+    return nat
+
+
+def test_forward_and_gradients_match_fp64_oracle(gpu):
+    import torch
+    from oracle import mlp_oracle as MO
+    from pypercolate_gb300.surrogate import MLP, WIDTHS
+    rng = np.random.default_rng(3)
+    model = MLP(seed=5)
+    B = 96
+    x = rng.normal(size=(B, 4)).astype(np.float32)
+    t = rng.normal(size=(B, 3)).astype(np.float32)
+    w = rng.uniform(0.5, 2.0, size=(B, 3)).astype(np.float32)
+    dx, dt, dw = (torch.from_numpy(a).cuda() for a in (x, t, w))
+    loss = float(model.loss_and_grads(dx, dt, dw))
+    y = model.forward_device(dx).cpu().numpy()
+    params = model.params.cpu().numpy()
+    y_ref, _, _ = MO.forward(params, WIDTHS, x)
+    np.testing.assert_allclose(y, y_ref, rtol=2e-5, atol=2e-5)
+    loss_ref, g_ref = MO.loss_and_grads(params, WIDTHS, x, t, w)
+    assert abs(loss - loss_ref) <= 1e-4 * abs(loss_ref)
+    g = model.grads.cpu().numpy()
+    assert g.shape == g_ref.shape
+    # products use identical BF16 operands: differences are FP32 accumulation only
+    scale = np.abs(g_ref).max()
+    np.testing.assert_allclose(g, g_ref, rtol=1e-3, atol=1e-4 * scale)
+
+
+def test_adam_matches_reference_update(gpu):
+    from pypercolate_gb300.surrogate import MLP
+    model = MLP(widths=(4, 8, 3), seed=1)
+    p0 = model.params.cpu().numpy().astype(np.float64)
+    model.grads.copy_(model.params * 0.5 + 0.1)
+    g = model.grads.cpu().numpy().astype(np.float64)
+    model.adam(lr=1e-3)
+    m = 0.1 * g
+    v = 0.001 * g * g
+    want = p0 - 1e-3 * (m / 0.1) / (np.sqrt(v / 0.001) + 1e-8)
+    np.testing.assert_allclose(model.params.cpu().numpy(), want, rtol=1e-5, atol=1e-7)
+
+
+def test_training_fits_a_smooth_function(gpu):
+    from pypercolate_gb300.surrogate import MLP
+    rng = np.random.default_rng(0)
+    X = rng.uniform(0, 1, size=(20000, 4)).astype(np.float32)
+    Y = np.column_stack([np.tanh(8 * (X[:, 0] - 0.5)), X[:, 1] ** 2, np.sin(3 * X[:, 2])])
+    model = MLP(seed=2)
+    trace = model.fit(X, Y, steps=400, batch=4096, lr=1e-3, log_every=100)
+    assert trace[-1][1] < 0.1 * trace[0][1]
+    pred = model.predict(X[:2000])
+    assert np.sqrt(np.mean((pred - Y[:2000]) ** 2)) < 0.1
+
+
+def test_surrogate_pipeline_small(gpu):
+    """Train on square lattices L in {8..48} minus 28, judge at L=28 by Monte
+    Carlo, and check that surrogate-placed p-grids interpolate the held-out
+    spanning curve better than a uniform grid of the same size."""
+    from pypercolate_gb300 import surrogate as S
+    ps = np.linspace(0.0, 1.0, 401)
+    X, Y = [], []
+    for L in (8, 12, 16, 20, 24, 32, 40, 48):
+        y, _ = S.ensemble_targets('grid', L, ps, 1500, key=L)
+        X.append(S.features(ps, L, 'grid'))
+        Y.append(y)
+    model = S.MLP(seed=0)
+    model.fit(np.concatenate(X), np.concatenate(Y), steps=1500, batch=4096, lr=1e-3)
+    dense = np.linspace(0.0, 1.0, 1001)
+    truth, truth_se = S.ensemble_targets('grid', 28, dense, 4000, key=2828)
+    pred = model.predict(S.features(dense, 28, 'grid'))
+    values, ok = S.judged(pred[:, 0], truth[:, 0], truth_se[:, 0])
+    assert np.all((values == pred[:, 0]) | (values == truth[:, 0]))
+    assert ok.mean() > 0.3  # most of the held-out curve is accepted
+    k = 16
+    uni = np.linspace(0.0, 1.0, k)
+    placed = S.place_p_grid(model, 28, 'grid', k)
+    err_uni = np.max(np.abs(np.interp(dense, uni, np.interp(uni, dense, truth[:, 0])) - truth[:, 0]))
+    err_placed = np.max(np.abs(np.interp(dense, placed, np.interp(placed, dense, truth[:, 0]))
+                               - truth[:, 0]))
+    assert err_placed < err_uni

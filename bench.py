@@ -53,7 +53,7 @@ def parse():
     ap.add_argument('--plain-chunk', type=int, default=4096)
     ap.add_argument('--mix-runs', type=int, default=1000000,
                     help='runs of the batched uneven workload (0: skip)')
-    ap.add_argument('--study', default=None, choices=[None, 'precision'],
+    ap.add_argument('--study', default=None, choices=[None, 'precision', 'surrogate'],
                     help='precision: FP32 vs FP64 canonical curves at L=1024 (separate line)')
     ap.add_argument('--l2-fetch', type=int, default=32,
                     help='L2 fetch granularity of this process (bytes; 0 = leave as is)')
@@ -238,12 +238,79 @@ def precision_study(args):
     return 0
 
 
+def surrogate_study(args):
+    """Train the MLP surrogate on ensembles at square lattices L in
+    {16..512} minus 384 and chains l in {1024..65536}, then judge it at the
+    held-out L = 384 against a Monte Carlo ensemble (2 standard errors), and
+    measure what its p-grid placement gains over a uniform grid."""
+    import torch
+    from pypercolate_gb300 import _native as nat
+    from pypercolate_gb300 import surrogate as S
+    torch.cuda.set_device(0)
+    if args.l2_fetch:
+        nat.set_l2_fetch_granularity(args.l2_fetch)
+    P = 52000
+    ps = np.linspace(0.0, 1.0, P)
+    lattices = [('grid', L) for L in (16, 24, 32, 48, 64, 96, 128, 192, 256, 320, 448, 512)] + \
+               [('chain', l) for l in (1024, 2048, 4096, 8192, 16384, 32768, 65536)]
+    t0 = time.perf_counter()
+    X, Y = [], []
+    for kind, L in lattices:
+        M = 2 * L * (L - 1) if kind == 'grid' else L - 1
+        runs = int(min(20000, max(1000, 2e9 / M)))
+        y, _ = S.ensemble_targets(kind, L, ps, runs, key=L)
+        X.append(S.features(ps, L, kind))
+        Y.append(y)
+    X, Y = np.concatenate(X), np.concatenate(Y)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    model = S.MLP(seed=0)
+    steps, batch = 12000, 4096
+    t0 = time.perf_counter()
+    trace = model.fit(X, Y, steps=steps, batch=batch, lr=1e-3, log_every=1000, decay=0.05)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    dense = np.linspace(0.0, 1.0, 2001)
+    truth, se = S.ensemble_targets('grid', 384, dense, 8000, key=384384)
+    pred = model.predict(S.features(dense, 384, 'grid'))
+    acc = {}
+    cheap, cheap_se = S.ensemble_targets('grid', 384, dense, 400, key=384400)
+    for j, name in enumerate(S.OUTPUTS):
+        _, ok = S.judged(pred[:, j], truth[:, j], se[:, j])
+        _, ok_c = S.judged(pred[:, j], cheap[:, j], cheap_se[:, j])
+        rms = float(np.sqrt(np.mean((pred[:, j] - truth[:, j]) ** 2)))
+        acc[name] = {'judge_8000_runs': float(ok.mean()), 'judge_400_runs': float(ok_c.mean()),
+                     'rms_error_vs_8000_runs': rms,
+                     'median_se_8000_runs': float(np.median(se[:, j]))}
+    gains = {}
+    for k in (16, 32, 64):
+        uni = np.linspace(0.0, 1.0, k)
+        placed = S.place_p_grid(model, 384, 'grid', k)
+        e_uni = float(np.max(np.abs(np.interp(dense, uni, np.interp(uni, dense, truth[:, 0]))
+                                    - truth[:, 0])))
+        e_pl = float(np.max(np.abs(np.interp(dense, placed, np.interp(placed, dense, truth[:, 0]))
+                                   - truth[:, 0])))
+        gains[k] = {'uniform_max_err': e_uni, 'surrogate_max_err': e_pl, 'ratio': e_uni / e_pl}
+    nxt, scores = S.pick_next_length(model, [352, 384, 416], 'grid', pilot_runs=500)
+    line = {'study': 'MLP surrogate', 'widths': list(S.WIDTHS), 'tuples': int(X.shape[0]),
+            'lattices': ['%s %d' % t for t in lattices], 'p_per_lattice': P,
+            'data_seconds': t_data, 'train_seconds': t_train, 'steps': steps, 'batch': batch,
+            'samples_per_s': steps * batch / t_train, 'loss_trace': trace,
+            'held_out': 'square L=384, 8000 runs, 2001 p',
+            'accepted_fraction_2se': acc, 'p_grid_gain_spanning': gains,
+            'next_length': {'choice': nxt, 'mean_abs_z': scores, 'candidates': [352, 384, 416]}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
     if args.study == 'precision':
         return precision_study(args)
+    if args.study == 'surrogate':
+        return surrogate_study(args)
     import torch
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)

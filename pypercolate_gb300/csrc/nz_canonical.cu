@@ -252,8 +252,11 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
     return fmaf((float)rec.m4_hi[off], 18446744073709551616.0f, u64_to_f32(rec.m4_lo[off]));
 }
 
-constexpr int kConvRuns = 128;  // runs per CTA (one per thread)
-constexpr int kConvPT = 16;     // probabilities per CTA
+#ifndef NZ_CONV_PT
+#define NZ_CONV_PT 16
+#endif
+constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
+constexpr int kConvPT = NZ_CONV_PT;    // probabilities per CTA
 constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before an FP64 flush
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the

@@ -43,11 +43,14 @@ def ensemble_targets(kind, L, ps, runs, key=11, run0=0, precision='fp32'):
     n = ca['number_of_runs'].astype(np.float64)
     se = lambda m2: np.sqrt(np.maximum(m2, 0.0) / np.maximum(n - 1, 1)) / np.sqrt(n)  # noqa: E731
     span = ca['percolation_probability_mean']
-    span_se = se(ca['percolation_probability_m2'])
+    # where every run agrees the sample error is 0; floor it at the binomial
+    # error of the Bayesian estimate (k+1)/(R+2) (one run's worth of doubt)
+    pb = (span * n + 1.0) / (n + 2.0)
+    span_se = np.maximum(se(ca['percolation_probability_m2']), np.sqrt(pb * (1 - pb) / n))
     strength = ca['max_cluster_size_mean'] / N
-    strength_se = se(ca['max_cluster_size_m2']) / N
+    strength_se = np.maximum(se(ca['max_cluster_size_m2']) / N, 1.0 / (N * np.sqrt(n)))
     chi = ca['moments_mean'][:, 2] / N
-    chi_se = se(ca['moments_m2'][:, 2]) / N
+    chi_se = np.maximum(se(ca['moments_m2'][:, 2]) / N, 1.0 / (N * np.sqrt(n)))
     floor = 1.0 / N ** 2
     log_chi = np.log(np.maximum(chi, floor))
     log_chi_se = chi_se / np.maximum(chi, floor)
@@ -138,8 +141,10 @@ class MLP:
             nat.ptr(self.params_bf16), self.count, lr, beta1, beta2, eps, self.step_count,
             nat.stream_handle()), 'nz_mlp_adam')
 
-    def fit(self, X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, log_every=0):
-        """Standardise, then Adam on shuffled mini-batches; returns the loss trace."""
+    def fit(self, X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, log_every=0, decay=0.0):
+        """Standardise, then Adam on random mini-batches; the learning rate
+        stays `lr`, then (decay > 0) falls geometrically to lr * decay over
+        the last third of the steps.  Returns the loss trace."""
         torch = nat.torch_cuda()
         X = np.asarray(X, np.float32)
         Y = np.asarray(Y, np.float32)
@@ -155,7 +160,10 @@ class MLP:
         for k in range(steps):
             idx = torch.randint(0, n, (batch,), device='cuda', generator=gen)
             loss = self.loss_and_grads(dX[idx].contiguous(), dY[idx].contiguous())
-            self.adam(lr)
+            rate = lr
+            if decay > 0.0 and k > 2 * steps // 3:
+                rate = lr * decay ** ((k - 2 * steps // 3) / max(1, steps - 2 * steps // 3))
+            self.adam(rate)
             if log_every and (k % log_every == 0 or k == steps - 1):
                 trace.append((k, float(loss)))
         return trace

@@ -250,7 +250,6 @@ def surrogate_study(args):
     if args.l2_fetch:
         nat.set_l2_fetch_granularity(args.l2_fetch)
     P = 52000
-    ps = np.linspace(0.0, 1.0, P)
     lattices = [('grid', L) for L in (16, 24, 32, 48, 64, 96, 128, 192, 256, 320, 448, 512)] + \
                [('chain', l) for l in (1024, 2048, 4096, 8192, 16384, 32768, 65536)]
     t0 = time.perf_counter()
@@ -258,8 +257,9 @@ def surrogate_study(args):
     for kind, L in lattices:
         M = 2 * L * (L - 1) if kind == 'grid' else L - 1
         runs = int(min(20000, max(1000, 2e9 / M)))
-        y, _ = S.ensemble_targets(kind, L, ps, runs, key=L)
-        X.append(S.features(ps, L, kind))
+        grid = S.training_grid(kind, L, P)
+        y, _ = S.ensemble_targets(kind, L, grid, runs, key=L)
+        X.append(S.features(grid, L, kind))
         Y.append(y)
     X, Y = np.concatenate(X), np.concatenate(Y)
     torch.cuda.synchronize()
@@ -294,6 +294,7 @@ def surrogate_study(args):
     nxt, scores = S.pick_next_length(model, [352, 384, 416], 'grid', pilot_runs=500)
     line = {'study': 'MLP surrogate', 'widths': list(S.WIDTHS), 'tuples': int(X.shape[0]),
             'lattices': ['%s %d' % t for t in lattices], 'p_per_lattice': P,
+            'p_grid': 'half uniform, half in the finite-size transition window',
             'data_seconds': t_data, 'train_seconds': t_train, 'steps': steps, 'batch': batch,
             'samples_per_s': steps * batch / t_train, 'loss_trace': trace,
             'held_out': 'square L=384, 8000 runs, 2001 p',

@@ -31,7 +31,9 @@ extern "C" {
 #define NZ_OK 0
 #define NZ_ERR_INVALID 1        /* invalid argument (Python: ValueError)       */
 #define NZ_ERR_SPANNING_SIDES 2 /* spanning requested, graph lacks two sides
-                                   (percolate/hpc.py:197-202: ValueError)     */
+                                   (percolate/hpc.py:197-202: ValueError);
+                                   reserved: the sides are graph attributes,
+                                   checked by the host layer before a call   */
 #define NZ_ERR_TOO_LARGE 3      /* beyond a documented size limit              */
 #define NZ_ERR_CUDA 4           /* a CUDA runtime call failed                  */
 #define NZ_ERR_WORKSPACE 5      /* workspace smaller than required             */
@@ -152,8 +154,9 @@ int nz_pack_microcanonical_rows(const NzRecords *rec, int32_t run,
  * 1067-1109 _binomial_pmf) in FP64 from log-binomials, for P values of p.
  * Band of p_i: n in [band_lo[i], band_lo[i] + band_len[i]), the n where
  * log B >= log B(mode) - cutoff; weights[i * cap + j] for j < band_len[i]
- * (zero-filled to cap).  Returns NZ_ERR_TOO_LARGE if a band exceeds cap.
- * nz_binomial_band_cap() is a safe cap for (M, cutoff). */
+ * (zero-filled to cap).  A band longer than cap is truncated to cap (no
+ * error: that would need a host synchronisation); nz_binomial_band_cap()
+ * returns a cap no band of (M, cutoff) exceeds. */
 int32_t nz_binomial_band_cap(uint32_t num_edges, double cutoff);
 int nz_binomial_weights(uint32_t num_edges, const double *ps, int32_t P,
                         double cutoff, int32_t cap, uint32_t *band_lo,

@@ -32,6 +32,20 @@ def features(ps, L, kind):
     return out
 
 
+def training_grid(kind, L, n):
+    """n probabilities for one lattice: half uniform in [0, 1], half inside
+    the finite-size transition window (square lattice: p_c = 1/2 +- 8 L^-3/4,
+    from nu = 4/3; chain: the last 8/l below p = 1), where the curves change
+    and a uniform grid puts almost no points."""
+    uni = np.linspace(0.0, 1.0, n - n // 2)
+    if kind == KIND_2D:
+        w = 8.0 * float(L) ** -0.75
+        win = np.linspace(max(0.0, 0.5 - w), min(1.0, 0.5 + w), n // 2)
+    else:
+        win = np.linspace(max(0.0, 1.0 - 8.0 / L), 1.0, n // 2)
+    return np.unique(np.concatenate([uni, win]))
+
+
 def ensemble_targets(kind, L, ps, runs, key=11, run0=0, precision='fp32'):
     """Monte Carlo estimates and standard errors of the three curves at ps,
     from one GPU ensemble (canonical averages of `runs` runs)."""

@@ -257,3 +257,39 @@ def test_student_t_quantile(gpu):
                                                      gpu.ptr(out), gpu.stream_handle()), 'tq')
     np.testing.assert_allclose(out.cpu().numpy(), scipy.stats.t.ppf(q, d), rtol=1e-10,
                                atol=1e-12)
+
+
+def test_banded_weights_and_record_convolution(gpu, oracle):
+    """nz_binomial_weights (banded FP64) and nz_canonical_statistics_records
+    (FP64 convolution of record planes) against the oracle."""
+    import torch
+    from pypercolate_gb300 import hpc
+    lib = gpu.lib_handle()
+    L, R = 16, 5
+    spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, L)
+    ps = np.array([0.0, 0.31, 0.5, 0.77, 1.0])
+    P = ps.size
+    cap = lib.nz_binomial_band_cap(spec.M, 80.0)
+    d_ps = torch.from_numpy(ps.copy()).cuda()
+    lo = torch.empty(P, dtype=torch.int32, device='cuda')
+    ln = torch.empty(P, dtype=torch.int32, device='cuda')
+    w = torch.empty(P * cap, dtype=torch.float64, device='cuda')
+    gpu.check(lib.nz_binomial_weights(spec.M, gpu.ptr(d_ps), P, 80.0, cap, gpu.ptr(lo),
+                                      gpu.ptr(ln), gpu.ptr(w), gpu.stream_handle()), 'weights')
+    W = w.cpu().numpy().reshape(P, cap)
+    lo_h, ln_h = lo.cpu().numpy(), ln.cpu().numpy()
+    for i, p in enumerate(ps):
+        full = np.zeros(spec.M + 1)
+        full[lo_h[i]:lo_h[i] + ln_h[i]] = W[i, :ln_h[i]]
+        np.testing.assert_allclose(full, oracle.binomial_pmf(spec.M, p), rtol=1e-11, atol=1e-33)
+    rec = hpc._run_microcanonical(spec, True, rng='philox', key=3, run0=0, n_runs=R,
+                                  with_edge=False)
+    out = torch.empty(R * P * 7, dtype=torch.float64, device='cuda')
+    gpu.check(lib.nz_canonical_statistics_records(rec.struct(), spec.N, spec.M, R, 1,
+                                                  gpu.ptr(lo), gpu.ptr(ln), gpu.ptr(w), cap, P,
+                                                  gpu.ptr(out), gpu.stream_handle()), 'conv')
+    got = out.cpu().numpy().reshape(R, P, 7)
+    Wfull = np.stack([oracle.binomial_pmf(spec.M, p) for p in ps])
+    for r in range(R):
+        q = oracle.q_matrix(oracle.lattice_run(0, L, oracle.philox_permutation(3, r, spec.M)))
+        np.testing.assert_allclose(got[r], Wfull @ q, rtol=1e-11, atol=1e-12)

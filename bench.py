@@ -32,6 +32,11 @@ KEY = 1234
 # random 32-byte sectors (find(u), find(v), the child pointer and the root
 # word written on a union) plus the 36 bytes of per-step records it streams
 UF_BYTES_PER_ADD = 4 * 32 + 36
+# measured DRAM bytes (read + write) per bond addition of uf_window_kernel:
+# ncu capture of spanning_2d_grid(256), 12,288 runs, one 1,024-row window at
+# p ~ 0.5 (profiles/window_kernels_L256_12288_runs.md); a full launch's
+# traffic is this figure times the additions it makes
+UF_TRAFFIC_PER_ADD = 206.5
 
 
 def parse():
@@ -463,7 +468,10 @@ def main():
                    'l2': 'inputs larger than L2 (%.1f GB of union-find state per step)'
                          % (R * N * 4 / 1e9)},
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
-                     'frac': achieved / peak, 'traffic': None,
+                     'frac': achieved / peak, 'traffic': UF_TRAFFIC_PER_ADD * adds_per_launch,
+                     'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum per '
+                                       'addition on a 12,288-run capture, scaled to the '
+                                       'launch by its additions',
                      'kernel': 'uf_window_kernel', 'peak_source': peak_kind,
                      'bytes_per_addition': UF_BYTES_PER_ADD,
                      'avg_launch_ms': uf_avg_s * 1e3},

@@ -42,6 +42,31 @@ extern "C" {
 #define NZ_GRAPH_GRID2D 0  /* spanning_2d_grid(L), percolate/percolate.py:931-965 */
 #define NZ_GRAPH_CHAIN1D 1 /* spanning_1d_chain(l), percolate/percolate.py:899-928 */
 #define NZ_GRAPH_EDGES 2   /* explicit edge list (any perc_graph)              */
+#define NZ_GRAPH_TORUS2D 3 /* L x L periodic square lattice: bond e < L*L joins
+                              node e = row*L + col to (row, col+1 mod L), bond
+                              e >= L*L joins node e - L*L to (row+1 mod L, col);
+                              N = L^2, M = 2 L^2.  The "spanning" flag of its
+                              records means that a cluster wraps around the
+                              torus (criterion: NZ_WRAP_*).  No counterpart in
+                              the reference.                                */
+#define NZ_KIND_MASK 0xFF
+
+/* Flags or'ed into NzGraph.kind: extensions that the reference lists as
+ * to-do (percolate/__init__.py:68-78; percolate/percolate.py:210-211 rejects
+ * any model but 'bond').
+ * NZ_MODEL_SITE: site percolation on GRID2D, CHAIN1D or TORUS2D -- step n
+ *   occupies the n-th site of a permutation of the N sites and joins it to
+ *   its occupied neighbours; the number of steps M is then N (nz_graph_size
+ *   reports it as num_edges, and every "M" below means the number of steps),
+ *   statistics count occupied sites only, and records carry `site` = 1.
+ * NZ_WRAP_*: TORUS2D only -- which wrapping sets the flag: a cluster that
+ *   wraps along x or y (EITHER, the default), along x (X), along y (Y), or
+ *   along both (BOTH), as in Newman & Ziff, Phys. Rev. E 64, 016706 (2001). */
+#define NZ_MODEL_SITE 0x100
+#define NZ_WRAP_EITHER 0x000
+#define NZ_WRAP_X 0x200
+#define NZ_WRAP_Y 0x400
+#define NZ_WRAP_BOTH 0x600
 
 /* ---- permutation sources -------------------------------------------- */
 #define NZ_PERM_PHILOX 0  /* Philox-4x32-10-keyed Feistel bijection: run r uses
@@ -77,8 +102,11 @@ typedef struct NzRecords {
     uint64_t *m3;       /* sum' s^3                                           */
     uint64_t *m4_lo;    /* sum' s^4, low 64 bits (the reference's uint64)     */
     uint32_t *m4_hi;    /* sum' s^4, bits 64..95                              */
-    uint32_t *edge;     /* edge index added at step n (0 at n = 0)            */
+    uint32_t *edge;     /* edge index added at step n (0 at n = 0); site
+                           index for site percolation                       */
     int64_t run_stride;
+    int32_t site;       /* 0: bond records (m1 = N - max); 1: site records
+                           (m1 = n - max: only occupied sites count)         */
 } NzRecords;
 
 /* ---- library -------------------------------------------------------- */
@@ -240,6 +268,22 @@ int nz_microcanonical_reduce(const NzRecords *rec, uint32_t num_nodes,
                              uint32_t num_edges, int32_t n_runs,
                              uint32_t n_begin, uint32_t n_end,
                              const NzMicroAccum *acc, void *stream);
+
+/* Merges two running states of independent run sets: dst <- dst (+) src.
+ * nz_canonical_merge: cols columns of (count, mean, M2) sharing one count per
+ * side -- the pairwise update that bond_reduce applies to two
+ * canonical_averages rows (percolate/hpc.py:638-702), here on the device
+ * arrays of nz_ensemble.  nz_micro_merge: the accumulators of two
+ * NzMicroAccum over num_edges + 1 rows (exact sums and spanning counts add,
+ * M2 merges pairwise).  Used to combine the shards of several GPUs or
+ * processes and checkpointed partial ensembles; dst and src must not alias.
+ * The reference merges such partial results through its task store
+ * (percolate/share/jugfile.py:240-244) with bond_reduce. */
+int nz_canonical_merge(uint64_t *dst_count, double *dst_mean, double *dst_m2,
+                       const uint64_t *src_count, const double *src_mean,
+                       const double *src_m2, int32_t cols, void *stream);
+int nz_micro_merge(const NzMicroAccum *dst, const NzMicroAccum *src,
+                   uint32_t num_edges, void *stream);
 
 /* Continues numpy's global MT19937 stream: state_in = 624 key words + the
  * position (np.random.get_state()); draws n_runs permutations of range(M) in

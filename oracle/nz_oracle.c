@@ -20,8 +20,8 @@
  *
  * Random permutations (three sources, all restated from published methods):
  *   - Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers:
- *     as easy as 1, 2, 3", SC'11) keys a balanced Feistel bijection with
- *     cycle walking: the project's permutation of [0, M).
+ *     as easy as 1, 2, 3", SC'11) keys an alternating Feistel bijection
+ *     with cycle walking: the project's permutation of [0, M).
  *   - MT19937 (Matsumoto & Nishimura, ACM TOMACS 8(1), 1998) with the
  *     authors' init_genrand / init_by_array seeding, followed by the
  *     Fisher-Yates shuffle with masked rejection sampling that numpy's legacy
@@ -69,9 +69,8 @@ void nzo_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2],
 /* Alternating Feistel network on b = bits(M-1) bits: left part floor(b/2)
  * bits, right part the rest; even rounds xor the left part with a keyed hash
  * of the right part, odd rounds the other way round; 8 rounds; the hash of a
- * v-bit value to o bits is the top o bits of hi32(((v << (32-v)) ^ k) *
- * 0xD2511F53).  Values >= M are re-encrypted (cycle walking), which keeps
- * the map a bijection on [0, M). */
+ * value v to o bits is the top o bits of lowbias32(v ^ k).  Values >= M are
+ * re-encrypted (cycle walking), which keeps the map a bijection on [0, M). */
 #define NZ_FEISTEL_ROUNDS 8
 #define NZ_PERM_TAG 0x5045524Du /* "PERM" */
 
@@ -100,19 +99,28 @@ void nzo_perm_init(nzo_perm_t *st, uint64_t key, uint64_t run_id, uint32_t M)
     }
 }
 
-static inline uint32_t nzo_feistel_f(uint32_t v, uint32_t vbits, uint32_t obits, uint32_t k)
+/* lowbias32: C. Wellons' xorshift-multiply integer hash (hash-prospector) */
+static inline uint32_t nzo_lowbias32(uint32_t x)
 {
-    uint32_t in = (vbits ? (v << (32u - vbits)) : 0u) ^ k;
-    uint32_t h = (uint32_t)(((uint64_t)in * PHILOX_M0) >> 32);
-    return obits ? (h >> (32u - obits)) : 0u;
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+static inline uint32_t nzo_feistel_f(uint32_t v, uint32_t obits, uint32_t k)
+{
+    return obits ? (nzo_lowbias32(v ^ k) >> (32u - obits)) : 0u;
 }
 
 static inline uint32_t nzo_feistel(const nzo_perm_t *st, uint32_t x)
 {
     uint32_t L = x >> st->hr, R = x & st->maskR;
     for (int i = 0; i < NZ_FEISTEL_ROUNDS; i += 2) {
-        L ^= nzo_feistel_f(R, st->hr, st->hl, st->k[i]) & st->maskL;
-        R ^= nzo_feistel_f(L, st->hl, st->hr, st->k[i + 1]) & st->maskR;
+        L ^= nzo_feistel_f(R, st->hl, st->k[i]) & st->maskL;
+        R ^= nzo_feistel_f(L, st->hr, st->k[i + 1]) & st->maskR;
     }
     return (L << st->hr) | R;
 }

@@ -35,10 +35,10 @@ _lib = None
 
 
 def build(force=False):
-    """Compile ``nz_oracle.c`` with the committed Makefile."""
-    src = os.path.join(HERE, 'nz_oracle.c')
+    """Compile ``nz_oracle.c`` and ``nz_census.c`` with the committed Makefile."""
+    srcs = [os.path.join(HERE, f) for f in ('nz_oracle.c', 'nz_census.c', 'Makefile')]
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(f) for f in srcs)):
         return LIB_PATH
     subprocess.check_call(['make', '-s', '-C', HERE])
     return LIB_PATH
@@ -72,6 +72,8 @@ def lib():
         L.nzo_ensemble_uf.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64,
                                       ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int]
         L.nzo_ensemble_uf.restype = ctypes.c_uint64
+        L.nzo_lattice_census.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                         u32p] + [ctypes.c_void_p] * 6
         _lib = L
     return _lib
 
@@ -317,3 +319,32 @@ def ensemble_uf(kind, L, key, run0, n_runs, n_threads=None):
         n_threads = os.cpu_count() or 1
     return int(lib().nzo_ensemble_uf(kind, int(L), int(key), int(run0), int(n_runs),
                                      int(n_threads)))
+
+
+CENSUS_KINDS = {'grid': 0, 'chain': 1, 'torus': 3}
+WRAP_CRITERIA = {'either': 0, 'x': 1, 'y': 2, 'both': 3}
+
+
+def census_size(kind, L, site):
+    """(N, number of steps) of a census lattice."""
+    N = L if kind == 'chain' else L * L
+    M = {'grid': 2 * L * (L - 1), 'chain': L - 1, 'torus': 2 * L * L}[kind]
+    return N, (N if site else M)
+
+
+def lattice_census(kind, L, perm, site=False, wrap='either'):
+    """Brute-force per-step records of one run (nz_census.c): dict of
+    max (with the spanning / wrapping flag in bit 31), m0, m2, m3, m4_lo,
+    m4_hi, each of length steps + 1."""
+    N, steps = census_size(kind, L, site)
+    perm = np.ascontiguousarray(perm, dtype=np.uint32)
+    assert perm.shape == (steps,)
+    out = {'max_span': np.zeros(steps + 1, np.uint32), 'm0': np.zeros(steps + 1, np.uint32),
+           'm2': np.zeros(steps + 1, np.uint64), 'm3': np.zeros(steps + 1, np.uint64),
+           'm4_lo': np.zeros(steps + 1, np.uint64), 'm4_hi': np.zeros(steps + 1, np.uint32)}
+    rc = lib().nzo_lattice_census(CENSUS_KINDS[kind], int(L), int(bool(site)), WRAP_CRITERIA[wrap],
+                                  _u32p(perm), *[out[k].ctypes.data_as(ctypes.c_void_p) for k in
+                                                 ('max_span', 'm0', 'm2', 'm3', 'm4_lo', 'm4_hi')])
+    if rc != 0:
+        raise ValueError('census failed for %s L=%d' % (kind, L))
+    return out

@@ -24,6 +24,10 @@ NZ_ERR_WORKSPACE = 5
 GRAPH_GRID2D = 0
 GRAPH_CHAIN1D = 1
 GRAPH_EDGES = 2
+GRAPH_TORUS2D = 3
+KIND_MASK = 0xFF
+MODEL_SITE = 0x100
+WRAP = {'either': 0x000, 'x': 0x200, 'y': 0x400, 'both': 0x600}
 
 PERM_PHILOX = 0
 PERM_GIVEN = 1
@@ -45,7 +49,7 @@ class NzGraph(ctypes.Structure):
 class NzRecords(ctypes.Structure):
     _fields_ = [('max_span', _vp), ('m0', _vp), ('m2', _vp), ('m3', _vp),
                 ('m4_lo', _vp), ('m4_hi', _vp), ('edge', _vp),
-                ('run_stride', ctypes.c_int64)]
+                ('run_stride', ctypes.c_int64), ('site', ctypes.c_int32)]
 
 
 class NzMicroAccum(ctypes.Structure):
@@ -110,6 +114,9 @@ _SIGNATURES = [
     ('nz_microcanonical_reduce', ctypes.c_int,
      [ctypes.POINTER(NzRecords), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
       ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(NzMicroAccum), _vp]),
+    ('nz_canonical_merge', ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp]),
+    ('nz_micro_merge', ctypes.c_int,
+     [ctypes.POINTER(NzMicroAccum), ctypes.POINTER(NzMicroAccum), ctypes.c_uint32, _vp]),
     ('nz_mt_stream_permutations', ctypes.c_int,
      [_vp, ctypes.c_uint32, ctypes.c_int32, _vp, _vp, _vp]),
     ('nz_student_t_quantile', ctypes.c_int, [_vp, _vp, ctypes.c_int32, _vp, _vp]),
@@ -281,9 +288,10 @@ def graph_size(g):
 class Records:
     """Device record planes for n_runs runs over `rows` rows (n-major)."""
 
-    def __init__(self, rows, n_runs, with_edge=False):
+    def __init__(self, rows, n_runs, with_edge=False, site=False):
         torch = torch_cuda()
         cnt = int(rows) * int(n_runs)
+        self.site = bool(site)
         self.rows = int(rows)
         self.n_runs = int(n_runs)
         self.max_span = torch.empty(max(cnt, 1), dtype=torch.int32, device='cuda')
@@ -304,6 +312,7 @@ class Records:
         r.m4_hi = self.m4_hi.data_ptr()
         r.edge = self.edge.data_ptr() if self.edge is not None else None
         r.run_stride = self.n_runs
+        r.site = int(self.site)
         return r
 
     def host(self):

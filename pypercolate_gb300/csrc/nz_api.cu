@@ -77,10 +77,11 @@ struct ProfScope {
 
 constexpr uint32_t kRecordBytes = 4 + 4 + 8 + 8 + 8 + 4;  // planes without edge
 
+
 // Workspace of the microcanonical entry point.
 size_t micro_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t perm_mode, uint32_t **nodes,
                     RunState **state, uint32_t **flag, uint32_t **perms) {
-    *nodes = c.take<uint32_t>((size_t)n_runs * g.N);
+    *nodes = c.take<uint32_t>((size_t)n_runs * g.N * node_words(g));
     *state = c.take<RunState>((size_t)n_runs);
     *flag = c.take<uint32_t>(4);
     *perms = perm_mode == NZ_PERM_MT19937 ? c.take<uint32_t>((size_t)n_runs * (g.M ? g.M : 1)) : nullptr;
@@ -331,6 +332,24 @@ int nz_microcanonical_reduce(const NzRecords *rec, uint32_t num_nodes, uint32_t 
     return check_launch();
 }
 
+int nz_canonical_merge(uint64_t *dst_count, double *dst_mean, double *dst_m2, const uint64_t *src_count,
+                       const double *src_mean, const double *src_m2, int32_t cols, void *stream) {
+    if (!dst_count || !src_count || cols < 0 || (cols > 0 && (!dst_mean || !dst_m2 || !src_mean || !src_m2)))
+        return NZ_ERR_INVALID;
+    if (dst_count == src_count) return NZ_ERR_INVALID;  // merging a state into itself
+    launch_canonical_merge(dst_count, dst_mean, dst_m2, src_count, src_mean, src_m2, cols, as_stream(stream));
+    return check_launch();
+}
+
+int nz_micro_merge(const NzMicroAccum *dst, const NzMicroAccum *src, uint32_t num_edges, void *stream) {
+    if (!dst || !src || num_edges >= 0xFFFFFFFFu) return NZ_ERR_INVALID;
+    if (!dst->count || !dst->span_count || !dst->sum_lo || !dst->sum_hi || !dst->m2) return NZ_ERR_INVALID;
+    if (!src->count || !src->span_count || !src->sum_lo || !src->sum_hi || !src->m2) return NZ_ERR_INVALID;
+    if (dst->count == src->count) return NZ_ERR_INVALID;
+    launch_micro_merge(*dst, *src, num_edges + 1u, as_stream(stream));
+    return check_launch();
+}
+
 int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges, int32_t n_runs, uint32_t *out,
                               uint32_t *state_out, void *stream) {
     if (!state_in || !state_out || n_runs <= 0 || (num_edges > 0 && !out)) return NZ_ERR_INVALID;
@@ -377,7 +396,7 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
                        EnsembleLayout &L) {
     L.window = pick_window(g.M, n_runs, window);
     L.cap = nz_binomial_band_cap(g.M, cutoff);
-    L.nodes = c.take<uint32_t>((size_t)n_runs * g.N);
+    L.nodes = c.take<uint32_t>((size_t)n_runs * g.N * node_words(g));
     L.state = c.take<RunState>((size_t)n_runs);
     L.flag = c.take<uint32_t>(4);
     const size_t plane = (size_t)L.window * n_runs;
@@ -389,6 +408,7 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     L.rec.m4_hi = c.take<uint32_t>(plane);
     L.rec.edge = nullptr;
     L.rec.run_stride = n_runs;
+    L.rec.site = (int32_t)g.site;
     L.band_lo = c.take<uint32_t>(P);
     L.band_len = c.take<uint32_t>(P);
     L.w64 = c.take<double>((size_t)P * L.cap);
@@ -476,7 +496,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         up.n_begin = w0; up.n_end = w1;
         {
             ProfScope prof(NZ_PROF_UNION_FIND, s);
-            launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, 128, s);
+            launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, 128, s);  // 64 and 256 per CTA: same time
         }
         if (micro) {
             ProfScope prof(NZ_PROF_MICRO, s);

@@ -253,7 +253,7 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
 }
 
 #ifndef NZ_CONV_PT
-#define NZ_CONV_PT 16
+#define NZ_CONV_PT 8
 #endif
 constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
 constexpr int kConvPT = NZ_CONV_PT;    // probabilities per CTA
@@ -264,7 +264,7 @@ constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before 
 // rows, with the tile's weights staged in shared memory (zero outside each
 // p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
 // products summed in FP32 over kConvChunk rows, then added into FP64.
-template <int PRECISION, int S>
+template <int PRECISION, int S, bool SITE>
 __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                           const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
                                           double *acc) {
@@ -275,8 +275,10 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
     const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
     for (uint32_t i = 0; i < cn; ++i) {
         const size_t off = base + (size_t)i * p.rec.run_stride;
-        const wtype q = PRECISION == 0 ? (wtype)record_value<S>(p.rec, off, p.N)
-                                       : (wtype)record_value_f<S>(p.rec, off, p.N);
+        // m1 = (sites in clusters) - max: N for bond records, n for site records
+        const uint32_t held = (S == 3 && SITE) ? c0 + i : p.N;
+        const wtype q = PRECISION == 0 ? (wtype)record_value<S>(p.rec, off, held)
+                                       : (wtype)record_value_f<S>(p.rec, off, held);
 #pragma unroll
         for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
     }
@@ -289,7 +291,7 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
 // rows, with the tile's weights staged in shared memory (zero outside each
 // p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
 // products summed in FP32 over kConvChunk rows, then added into FP64.
-template <int PRECISION>
+template <int PRECISION, bool SITE>
 __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     __shared__ wtype s_w[kConvChunk][kConvPT];
@@ -335,13 +337,13 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
         __syncthreads();
         if (r < p.n_runs) {
             switch (s) {
-                case 0: conv_rows<PRECISION, 0>(p, c0, cn, r, s_w, acc); break;
-                case 1: conv_rows<PRECISION, 1>(p, c0, cn, r, s_w, acc); break;
-                case 2: conv_rows<PRECISION, 2>(p, c0, cn, r, s_w, acc); break;
-                case 3: conv_rows<PRECISION, 3>(p, c0, cn, r, s_w, acc); break;
-                case 4: conv_rows<PRECISION, 4>(p, c0, cn, r, s_w, acc); break;
-                case 5: conv_rows<PRECISION, 5>(p, c0, cn, r, s_w, acc); break;
-                default: conv_rows<PRECISION, 6>(p, c0, cn, r, s_w, acc); break;
+                case 0: conv_rows<PRECISION, 0, SITE>(p, c0, cn, r, s_w, acc); break;
+                case 1: conv_rows<PRECISION, 1, SITE>(p, c0, cn, r, s_w, acc); break;
+                case 2: conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc); break;
+                case 3: conv_rows<PRECISION, 3, SITE>(p, c0, cn, r, s_w, acc); break;
+                case 4: conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc); break;
+                case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
+                default: conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc); break;
             }
         }
     }
@@ -357,8 +359,15 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
 void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
     dim3 grid((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 7);
-    if (precision == 0) conv_window_kernel<0><<<grid, kConvRuns, 0, s>>>(p);
-    else conv_window_kernel<1><<<grid, kConvRuns, 0, s>>>(p);
+    // the record model is a template parameter: a run-time test in the row
+    // loop cost 17 % of the kernel's time
+    if (p.rec.site) {
+        if (precision == 0) conv_window_kernel<0, true><<<grid, kConvRuns, 0, s>>>(p);
+        else conv_window_kernel<1, true><<<grid, kConvRuns, 0, s>>>(p);
+    } else {
+        if (precision == 0) conv_window_kernel<0, false><<<grid, kConvRuns, 0, s>>>(p);
+        else conv_window_kernel<1, false><<<grid, kConvRuns, 0, s>>>(p);
+    }
 }
 
 __global__ void f64_to_f32_kernel(const double *a, float *b, size_t n) {
@@ -607,7 +616,8 @@ __global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
         return v > 0.0 ? v : 0.0;
     };
     // statistic order 0 max, 1 m0, 2 m1 (= N - max: same M2 as max), 3 m2, 4 m3, 5 m4
-    const u128 sx[6] = {sx_max, sx_m0, (u128)Rn * p.N - sx_max, sx_m2, sx_m3, sx_m4};
+    const u128 held = rec.site ? n : p.N;  // sites in clusters: all N (bond) or the n occupied (site)
+    const u128 sx[6] = {sx_max, sx_m0, (u128)Rn * held - sx_max, sx_m2, sx_m3, sx_m4};
     const double m2b_max = m2_exact(sq_max, sd_max);
     const double m2b[6] = {m2b_max, m2_exact(sq_m0, sd_m0), m2b_max, m2_exact(sq_m2, sd_m2),
                            m2_float(fq_m3, sd_m3), m2_float(fq_m4, sd_m4)};
@@ -634,6 +644,61 @@ void launch_micro_window(const MicroParams &p, cudaStream_t s) {
 
 void launch_micro_count(uint64_t *count, int32_t n_runs, cudaStream_t s) {
     add_count_kernel<<<1, 1, 0, s>>>(count, n_runs);
+}
+
+// ------------------------------------------------ merging two accumulators
+// dst <- dst (+) src for running (count, mean, M2) columns sharing one count
+// each side: the pairwise update of percolate/hpc.py:638-702.
+__global__ void canonical_merge_kernel(const uint64_t *dst_count, double *dst_mean, double *dst_m2,
+                                       const uint64_t *src_count, const double *src_mean,
+                                       const double *src_m2, int32_t cols) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    double na = (double)*dst_count, ma = dst_mean[c], sa = dst_m2[c];
+    chan_merge(na, ma, sa, (double)*src_count, src_mean[c], src_m2[c]);
+    dst_mean[c] = ma;
+    dst_m2[c] = sa;
+}
+
+// Microcanonical accumulators of rows = M + 1 rows: exact 128-bit sums and
+// spanning counts add; M2 merges pairwise with the means taken from the
+// exact sums, as micro_window_kernel merges a batch.
+__global__ void micro_merge_kernel(NzMicroAccum dst, NzMicroAccum src, uint32_t rows) {
+    const size_t total = (size_t)6 * rows;
+    const double na = (double)*dst.count, nb = (double)*src.count;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total + rows;
+         i += (size_t)gridDim.x * blockDim.x) {
+        if (i >= total) {
+            dst.span_count[i - total] += src.span_count[i - total];
+            continue;
+        }
+        const u128 a = ((u128)dst.sum_hi[i] << 64) | dst.sum_lo[i];
+        const u128 b = ((u128)src.sum_hi[i] << 64) | src.sum_lo[i];
+        double nn = na, mm = na > 0 ? u128_to_f64(a) / na : 0.0, ss = dst.m2[i];
+        chan_merge(nn, mm, ss, nb, nb > 0 ? u128_to_f64(b) / nb : 0.0, src.m2[i]);
+        const u128 t = a + b;
+        dst.sum_lo[i] = (uint64_t)t;
+        dst.sum_hi[i] = (uint64_t)(t >> 64);
+        dst.m2[i] = ss;
+    }
+}
+
+__global__ void add_counts_kernel(uint64_t *dst, const uint64_t *src) { *dst += *src; }
+
+// the counts are read by the merge kernels, so they are added afterwards
+void launch_canonical_merge(uint64_t *dst_count, double *dst_mean, double *dst_m2, const uint64_t *src_count,
+                            const double *src_mean, const double *src_m2, int32_t cols, cudaStream_t s) {
+    if (cols > 0)
+        canonical_merge_kernel<<<(cols + 255) / 256, 256, 0, s>>>(dst_count, dst_mean, dst_m2, src_count,
+                                                                  src_mean, src_m2, cols);
+    add_counts_kernel<<<1, 1, 0, s>>>(dst_count, src_count);
+}
+
+void launch_micro_merge(const NzMicroAccum &dst, const NzMicroAccum &src, uint32_t rows, cudaStream_t s) {
+    const size_t work = (size_t)7 * rows;
+    const unsigned grid = (unsigned)((work + 255) / 256 < 4096 ? (work + 255) / 256 : 4096);
+    micro_merge_kernel<<<grid, 256, 0, s>>>(dst, src, rows);
+    add_counts_kernel<<<1, 1, 0, s>>>(dst.count, src.count);
 }
 
 // =====================================================================

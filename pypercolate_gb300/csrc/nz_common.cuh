@@ -61,16 +61,29 @@ __host__ __device__ inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 // left part of floor(b/2) bits and a right part of the remaining bits; round
 // i xors one part with a keyed hash of the other (even rounds update the
 // left part, odd rounds the right part), 8 rounds, round keys from two
-// Philox-4x32-10 blocks.  Values >= M are re-encrypted (cycle walking); the
-// domain is < 2M so fewer than 2 walks are needed on average, and about one
-// for spanning_2d_grid(2^k), whose M = 2L(L-1) lies just below 2^b.
+// Philox-4x32-10 blocks.  The round function is the top bits of
+// lowbias32(v ^ k), C. Wellons' two-multiply xorshift integer hash
+// (hash-prospector, 2018), whose output bits all depend on all input bits: a
+// single multiply-high instead makes the network nearly affine, and the
+// permutation then over-represents parts of the edge range in its prefixes
+// (7x the hypergeometric spread of the horizontal-bond share of a torus).
+// Values >= M are re-encrypted (cycle walking); the domain is < 2M so fewer
+// than 2 walks are needed on average, and about one for
+// spanning_2d_grid(2^k), whose M = 2L(L-1) lies just below 2^b.
 constexpr int kFeistelRounds = 8;
 constexpr uint32_t kPermTag = 0x5045524Du;  // "PERM"
 
-__host__ __device__ __forceinline__ uint32_t feistel_f(uint32_t v, uint32_t vbits, uint32_t obits, uint32_t k) {
-    const uint32_t in = (vbits ? (v << (32u - vbits)) : 0u) ^ k;
-    const uint32_t h = (uint32_t)(((uint64_t)in * kPhiloxM0) >> 32);
-    return obits ? (h >> (32u - obits)) : 0u;
+__host__ __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__host__ __device__ __forceinline__ uint32_t feistel_f(uint32_t v, uint32_t obits, uint32_t k) {
+    return obits ? (lowbias32(v ^ k) >> (32u - obits)) : 0u;
 }
 
 struct FeistelPerm {
@@ -101,8 +114,8 @@ struct FeistelPerm {
         uint32_t L = x >> hr, R = x & maskR;
 #pragma unroll
         for (int i = 0; i < kFeistelRounds; i += 2) {
-            L ^= feistel_f(R, hr, hl, k[i]) & maskL;
-            R ^= feistel_f(L, hl, hr, k[i + 1]) & maskR;
+            L ^= feistel_f(R, hl, k[i]) & maskL;
+            R ^= feistel_f(L, hr, k[i + 1]) & maskR;
         }
         return (L << hr) | R;
     }
@@ -117,7 +130,9 @@ struct FeistelPerm {
 
 // ------------------------------------------------------------- graphs
 struct GraphDev {
-    int32_t kind;
+    int32_t kind;         // NZ_GRAPH_* without flags
+    uint32_t site;        // NZ_MODEL_SITE given: M = N steps occupy sites
+    uint32_t wrap;        // torus: NZ_WRAP_* >> 9 (0 either, 1 x, 2 y, 3 both)
     uint32_t L, N, M;
     uint32_t row_edges;   // grid: (L-1)*(2L-1) edges in rows 0..L-2
     uint32_t two_l_m1;    // grid: 2L-1
@@ -126,21 +141,40 @@ struct GraphDev {
     const uint8_t *side;
 };
 
+inline int graph_size_base(const NzGraph &g, int kind, uint32_t &N, uint32_t &M);
+
 inline int graph_size(const NzGraph &g, uint32_t &N, uint32_t &M) {
-    if (g.kind == NZ_GRAPH_GRID2D) {
+    const int kind = g.kind & NZ_KIND_MASK, flags = g.kind & ~NZ_KIND_MASK;
+    if (flags & ~(NZ_MODEL_SITE | NZ_WRAP_BOTH)) return NZ_ERR_INVALID;
+    if ((flags & NZ_WRAP_BOTH) && kind != NZ_GRAPH_TORUS2D) return NZ_ERR_INVALID;
+    if ((flags & NZ_MODEL_SITE) && kind == NZ_GRAPH_EDGES) return NZ_ERR_INVALID;
+    const int st = graph_size_base(g, kind, N, M);
+    if (st == NZ_OK && (flags & NZ_MODEL_SITE)) M = N;
+    return st;
+}
+
+inline int graph_size_base(const NzGraph &g, int kind, uint32_t &N, uint32_t &M) {
+    if (kind == NZ_GRAPH_TORUS2D) {
+        if (g.length == 0) return NZ_ERR_INVALID;
+        if ((uint64_t)g.length * g.length > NZ_MAX_NODES) return NZ_ERR_TOO_LARGE;
+        N = g.length * g.length;
+        M = 2u * N;
+        return NZ_OK;
+    }
+    if (kind == NZ_GRAPH_GRID2D) {
         if (g.length == 0 || (uint64_t)g.length * g.length > NZ_MAX_NODES) return NZ_ERR_TOO_LARGE;
         N = g.length * g.length;
         M = 2u * g.length * (g.length - 1u);
         return NZ_OK;
     }
-    if (g.kind == NZ_GRAPH_CHAIN1D) {
+    if (kind == NZ_GRAPH_CHAIN1D) {
         if (g.length == 0) return NZ_ERR_INVALID;
         if (g.length > NZ_MAX_NODES) return NZ_ERR_TOO_LARGE;
         N = g.length;
         M = g.length - 1u;
         return NZ_OK;
     }
-    if (g.kind == NZ_GRAPH_EDGES) {
+    if (kind == NZ_GRAPH_EDGES) {
         if (g.num_nodes == 0) return NZ_ERR_INVALID;
         if (g.num_nodes > NZ_MAX_NODES || g.num_edges > 2u * NZ_MAX_NODES) return NZ_ERR_TOO_LARGE;
         if (g.num_edges > 0 && (!g.edge_u || !g.edge_v)) return NZ_ERR_INVALID;
@@ -153,14 +187,16 @@ inline int graph_size(const NzGraph &g, uint32_t &N, uint32_t &M) {
 
 inline GraphDev make_graph_dev(const NzGraph &g, uint32_t N, uint32_t M) {
     GraphDev d;
-    d.kind = g.kind;
+    d.kind = g.kind & NZ_KIND_MASK;
+    d.site = (g.kind & NZ_MODEL_SITE) ? 1u : 0u;
+    d.wrap = (uint32_t)(g.kind & NZ_WRAP_BOTH) >> 9;
     d.L = g.length;
     d.N = N;
     d.M = M;
     d.row_edges = 0;
     d.two_l_m1 = 1;
     d.inv_two_l_m1 = 1.0f;
-    if (g.kind == NZ_GRAPH_GRID2D) {
+    if (d.kind == NZ_GRAPH_GRID2D) {
         d.two_l_m1 = 2u * g.length - 1u;
         d.row_edges = (g.length - 1u) * d.two_l_m1;
         d.inv_two_l_m1 = 1.0f / (float)d.two_l_m1;
@@ -225,5 +261,13 @@ struct __align__(16) RunState {
 constexpr uint32_t kFlagSpan = 1u;
 constexpr uint32_t kFlagInitBoth = 2u;
 constexpr uint32_t kFlagCorrupt = 4u;   // a find exceeded the depth bound (never in valid use)
+constexpr uint32_t kFlagWrapX = 8u;     // torus: a cluster wraps along x
+constexpr uint32_t kFlagWrapY = 16u;    // torus: a cluster wraps along y
+
+// 32-bit words of union-find state per node: the torus kernels keep the
+// node word and the displacement (dx, dy) to the parent in one 16-byte cell
+__host__ __device__ __forceinline__ uint32_t node_words(const GraphDev &g) {
+    return g.kind == NZ_GRAPH_TORUS2D ? 4u : 1u;
+}
 
 }  // namespace nz

@@ -13,7 +13,7 @@ namespace nz {
 struct UfParams {
     GraphDev g;
     int32_t n_runs;
-    uint32_t *nodes;        // [n_runs][N]
+    uint32_t *nodes;        // [n_runs][N * node_words(g)]
     RunState *state;        // [n_runs]
     uint32_t n_begin;       // rows emitted: [n_begin, n_end)
     uint32_t n_end;
@@ -34,6 +34,12 @@ void launch_mt_stream_perms(const uint32_t *state_in, uint32_t M, int32_t n_runs
                             uint32_t *state_out, cudaStream_t s);
 void launch_pack_rows(const NzRecords &rec, int32_t run, uint32_t N, uint32_t M, int32_t spanning,
                       uint8_t *rows, cudaStream_t s);
+
+// nz_lattice.cu: site percolation and the torus (dispatched from nz_uf.cu)
+bool lattice_extension(const GraphDev &g);
+void launch_init_lattice_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,
+                              cudaStream_t s);
+void launch_lattice_window(const UfParams &p, int perm_mode, bool span, int block, cudaStream_t s);
 
 // nz_canonical.cu
 void launch_binomial_weights(uint32_t M, const double *ps, int32_t P, double cutoff, int32_t cap,
@@ -72,6 +78,9 @@ struct MicroParams {
 };
 void launch_micro_window(const MicroParams &p, cudaStream_t s);
 void launch_micro_count(uint64_t *count, int32_t n_runs, cudaStream_t s);
+void launch_canonical_merge(uint64_t *dst_count, double *dst_mean, double *dst_m2, const uint64_t *src_count,
+                            const double *src_mean, const double *src_m2, int32_t cols, cudaStream_t s);
+void launch_micro_merge(const NzMicroAccum &dst, const NzMicroAccum &src, uint32_t rows, cudaStream_t s);
 
 void launch_init_avg(const uint8_t *canon_rows, int32_t P, int32_t spanning, uint8_t *out, cudaStream_t s);
 void launch_bond_reduce(const uint8_t *a, const uint8_t *b, int32_t P, int32_t spanning, uint8_t *out,

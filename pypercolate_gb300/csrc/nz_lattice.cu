@@ -1,0 +1,349 @@
+// nz_lattice.cu -- site percolation, and wrapping on the periodic square lattice.
+//
+// Extensions that the reference lists as to-do (percolate/__init__.py:68-78;
+// percolate/percolate.py:210-211 rejects every model but 'bond'), built on
+// the union-find of nz_uf.cu and writing the same per-step records, so the
+// fused microcanonical reductions, the canonical convolution and every other
+// consumer of records apply unchanged.
+//
+// Site percolation (Newman & Ziff, Phys. Rev. Lett. 85, 4104 (2000); Phys.
+// Rev. E 64, 016706 (2001), Sec. II): step n occupies the n-th site of a
+// permutation of the N sites -- a new cluster of one site -- and joins it to
+// each occupied neighbour.  An unoccupied site holds the root word of size 0.
+// The statistics count occupied sites only (T_k over occupied clusters, so
+// m1 = n - max; m0 = clusters - 1, or 0 while no site is occupied).
+//
+// Wrapping (NZ 2001, Sec. III.B): on the L x L torus every node keeps, next to
+// its union-find word, its displacement (dx, dy) from its parent, so a find
+// returns the root and the node's position relative to it.  Joining u to
+// v = u + delta inside one cluster closes a loop, which winds around the
+// torus exactly when pos(u) + delta != pos(v): along x when the x parts
+// differ, along y when the y parts differ.  A union hangs one root below the
+// other with the displacement that keeps pos(v) = pos(u) + delta.  Positions
+// are exact in 32-bit integers: each is a sum of at most N - 1 unit steps
+// along the clusters' spanning trees.  The run's wrap flags are sticky, like
+// the spanning flag; two clusters cannot wrap along different directions (the
+// loops would cross), so "along both" is the conjunction of the two flags.
+#include <cstdint>
+
+#include "nz_common.cuh"
+#include "nz_internal.cuh"
+
+namespace nz {
+
+namespace {
+
+__device__ __forceinline__ void add128(uint64_t &lo, uint64_t &hi, uint64_t blo, uint64_t bhi) {
+    uint64_t nlo = lo + blo;
+    hi += bhi + (nlo < lo ? 1ull : 0ull);
+    lo = nlo;
+}
+
+constexpr uint32_t kEmpty = kRoot;  // make_root(0, 0): an unoccupied site
+
+// Exact T_k of all clusters and the powers of the largest size.
+struct Tally {
+    RunState st;
+    uint32_t mx;
+    uint64_t mx2, mx3, mx4_lo, mx4_hi;
+
+    __device__ void load(const RunState &s) {
+        st = s;
+        mx = s.max;
+        powers();
+    }
+    __device__ __forceinline__ void powers() {
+        mx2 = (uint64_t)mx * mx;
+        mx3 = mx2 * mx;
+        mx4_lo = mx3 * mx;
+        mx4_hi = __umul64hi(mx3, (uint64_t)mx);
+    }
+    // a new cluster of one site
+    __device__ __forceinline__ void add_single() {
+        st.t0 += 1u;
+        st.t2 += 1u;
+        st.t3 += 1u;
+        add128(st.t4_lo, st.t4_hi, 1u, 0u);
+        if (mx < 1u) { mx = 1u; powers(); }
+    }
+    // clusters of sizes a and b become one
+    __device__ __forceinline__ void merge(uint32_t a, uint32_t b) {
+        const uint32_t s = a + b;
+        st.t0 -= 1u;
+        const uint64_t ab = (uint64_t)a * b;
+        st.t2 += 2ull * ab;
+        st.t3 += 3ull * ab * s;
+        const uint64_t q = 4ull * a * a + 6ull * ab + 4ull * b * b;
+        add128(st.t4_lo, st.t4_hi, ab * q, __umul64hi(ab, q));
+        if (s > mx) { mx = s; powers(); }
+    }
+    // row n of the records
+    __device__ __forceinline__ void write(const NzRecords &rec, size_t off, bool flag, uint32_t e) const {
+        if (rec.max_span) rec.max_span[off] = mx | (flag ? kSpanBit : 0u);
+        if (rec.m0) rec.m0[off] = st.t0 - (st.t0 ? 1u : 0u);
+        if (rec.m2) rec.m2[off] = st.t2 - mx2;
+        if (rec.m3) rec.m3[off] = st.t3 - mx3;
+        const uint64_t m4_lo = st.t4_lo - mx4_lo;
+        const uint64_t m4_hi = st.t4_hi - mx4_hi - (st.t4_lo < mx4_lo ? 1ull : 0ull);
+        if (rec.m4_lo) rec.m4_lo[off] = m4_lo;
+        if (rec.m4_hi) rec.m4_hi[off] = (uint32_t)m4_hi;
+        if (rec.edge) rec.edge[off] = e;
+    }
+};
+
+template <int PERM>
+__device__ __forceinline__ uint32_t step_index(const FeistelPerm &fp, const uint32_t *perm, uint32_t idx) {
+    return PERM == NZ_PERM_PHILOX ? fp.at(idx) : __ldg(perm + idx);
+}
+
+// ------------------------------------------------- grid / chain, site model
+// Joins the clusters of u and v (interleaved finds with path splitting, union
+// by size); the joined root's side set decides spanning.
+template <bool SPAN>
+__device__ __forceinline__ void link(uint32_t *node, uint32_t u, uint32_t v, Tally &t) {
+    uint32_t xu = u, xv = v;
+    uint32_t wu = node[xu], wv = node[xv];
+    for (int hops = 0; !(is_root(wu) && is_root(wv)); ++hops) {
+        if (hops >= 64) { t.st.flags |= kFlagCorrupt; return; }
+        if (!is_root(wu)) {
+            const uint32_t nu = node[wu];
+            if (!is_root(nu)) node[xu] = nu;
+            xu = wu; wu = nu;
+        }
+        if (!is_root(wv)) {
+            const uint32_t nv = node[wv];
+            if (!is_root(nv)) node[xv] = nv;
+            xv = wv; wv = nv;
+        }
+    }
+    if (xu == xv) return;
+    const uint32_t a = root_size(wu), b = root_size(wv);
+    const uint32_t sides = root_sides(wu) | root_sides(wv);
+    uint32_t big = xu, small = xv;
+    if (a < b) { big = xv; small = xu; }
+    node[small] = big;
+    node[big] = make_root(a + b, sides);
+    t.merge(a, b);
+    if (SPAN && sides == 3u) t.st.flags |= kFlagSpan;
+}
+
+template <int KIND, int PERM, bool SPAN>
+__global__ void __launch_bounds__(256) site_window_kernel(UfParams p) {
+    const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p.n_runs) return;
+    const GraphDev &g = p.g;
+    uint32_t *node = p.nodes + (size_t)r * g.N;
+    Tally t;
+    t.load(p.state[r]);
+    FeistelPerm fp;
+    const uint32_t *perm = nullptr;
+    if (PERM == NZ_PERM_PHILOX) fp.init(p.key, p.run0 + (uint64_t)r, g.M);
+    else perm = p.perms + (size_t)r * g.M;
+    const NzRecords rec = p.rec;
+    for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
+        uint32_t i = 0;
+        if (n > 0) {
+            i = step_index<PERM>(fp, perm, n - 1u);
+            // a caller-supplied index out of range or repeated occupies nothing
+            if (i < g.N && node[i] == kEmpty) {
+                const uint32_t sides = node_sides<KIND>(g, i);
+                node[i] = make_root(1u, sides);
+                t.add_single();
+                if (SPAN && sides == 3u) t.st.flags |= kFlagSpan;
+                if (KIND == NZ_GRAPH_GRID2D) {
+                    const uint32_t row = i / g.L, col = i - row * g.L;
+                    if (row > 0 && node[i - g.L] != kEmpty) link<SPAN>(node, i, i - g.L, t);
+                    if (row + 1u < g.L && node[i + g.L] != kEmpty) link<SPAN>(node, i, i + g.L, t);
+                    if (col > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
+                    if (col + 1u < g.L && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
+                } else {
+                    if (i > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
+                    if (i + 1u < g.N && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
+                }
+            }
+        }
+        const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
+        t.write(rec, off, SPAN && (t.st.flags & kFlagSpan), i);
+    }
+    t.st.max = t.mx;
+    p.state[r] = t.st;
+}
+
+// ------------------------------------------------------ torus with wrapping
+// cell: x = union-find word, y = dx, z = dy (two's complement), w unused
+__device__ __forceinline__ bool wraps(uint32_t flags, uint32_t crit) {
+    const bool x = (flags & kFlagWrapX) != 0, y = (flags & kFlagWrapY) != 0;
+    return crit == 0 ? (x || y) : crit == 1 ? x : crit == 2 ? y : (x && y);
+}
+
+// Joins u and v = u + (ddx, ddy); interleaved finds with path splitting that
+// keep each node's displacement from its parent.
+__device__ __forceinline__ void link_torus(uint4 *cell, uint32_t u, uint32_t v, int32_t ddx, int32_t ddy,
+                                           Tally &t) {
+    uint32_t xu = u, xv = v;
+    uint4 cu = cell[xu], cv = cell[xv];
+    int32_t pux = 0, puy = 0, pvx = 0, pvy = 0;  // positions relative to the current node
+    for (int hops = 0; !(is_root(cu.x) && is_root(cv.x)); ++hops) {
+        if (hops >= 64) { t.st.flags |= kFlagCorrupt; return; }
+        if (!is_root(cu.x)) {
+            const uint32_t par = cu.x;
+            const uint4 cp = cell[par];
+            pux += (int32_t)cu.y;
+            puy += (int32_t)cu.z;
+            if (!is_root(cp.x)) cell[xu] = make_uint4(cp.x, cu.y + cp.y, cu.z + cp.z, 0u);
+            xu = par;
+            cu = cp;
+        }
+        if (!is_root(cv.x)) {
+            const uint32_t par = cv.x;
+            const uint4 cp = cell[par];
+            pvx += (int32_t)cv.y;
+            pvy += (int32_t)cv.z;
+            if (!is_root(cp.x)) cell[xv] = make_uint4(cp.x, cv.y + cp.y, cv.z + cp.z, 0u);
+            xv = par;
+            cv = cp;
+        }
+    }
+    // position of v's root as seen from u's root, were v at pos(u) + delta
+    const int32_t ox = pux + ddx - pvx, oy = puy + ddy - pvy;
+    if (xu == xv) {
+        if (ox != 0) t.st.flags |= kFlagWrapX;
+        if (oy != 0) t.st.flags |= kFlagWrapY;
+        return;
+    }
+    const uint32_t a = root_size(cu.x), b = root_size(cv.x);
+    if (a >= b) {
+        cell[xv] = make_uint4(xu, (uint32_t)ox, (uint32_t)oy, 0u);
+        cell[xu] = make_uint4(make_root(a + b, 0u), 0u, 0u, 0u);
+    } else {
+        cell[xu] = make_uint4(xv, (uint32_t)(-ox), (uint32_t)(-oy), 0u);
+        cell[xv] = make_uint4(make_root(a + b, 0u), 0u, 0u, 0u);
+    }
+    t.merge(a, b);
+}
+
+template <bool SITE, int PERM, bool SPAN>
+__global__ void __launch_bounds__(256) torus_window_kernel(UfParams p) {
+    const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p.n_runs) return;
+    const GraphDev &g = p.g;
+    uint4 *cell = reinterpret_cast<uint4 *>(p.nodes) + (size_t)r * g.N;
+    Tally t;
+    t.load(p.state[r]);
+    FeistelPerm fp;
+    const uint32_t *perm = nullptr;
+    if (PERM == NZ_PERM_PHILOX) fp.init(p.key, p.run0 + (uint64_t)r, g.M);
+    else perm = p.perms + (size_t)r * g.M;
+    const NzRecords rec = p.rec;
+    const uint32_t L = g.L;
+    for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
+        uint32_t e = 0;
+        if (n > 0) {
+            e = step_index<PERM>(fp, perm, n - 1u);
+            if (SITE) {
+                if (e < g.N && cell[e].x == kEmpty) {
+                    cell[e] = make_uint4(make_root(1u, 0u), 0u, 0u, 0u);
+                    t.add_single();
+                    const uint32_t row = e / L, col = e - row * L;
+                    const uint32_t right = row * L + (col + 1u == L ? 0u : col + 1u);
+                    const uint32_t left = row * L + (col == 0u ? L - 1u : col - 1u);
+                    const uint32_t down = (row + 1u == L ? 0u : row + 1u) * L + col;
+                    const uint32_t up = (row == 0u ? L - 1u : row - 1u) * L + col;
+                    if (cell[right].x != kEmpty) link_torus(cell, e, right, 1, 0, t);
+                    if (cell[left].x != kEmpty) link_torus(cell, e, left, -1, 0, t);
+                    if (cell[down].x != kEmpty) link_torus(cell, e, down, 0, 1, t);
+                    if (cell[up].x != kEmpty) link_torus(cell, e, up, 0, -1, t);
+                }
+            } else if (e < g.M) {
+                const bool vertical = e >= g.N;
+                const uint32_t u = vertical ? e - g.N : e;
+                const uint32_t row = u / L, col = u - row * L;
+                const uint32_t v = vertical ? (row + 1u == L ? 0u : row + 1u) * L + col
+                                            : row * L + (col + 1u == L ? 0u : col + 1u);
+                link_torus(cell, u, v, vertical ? 0 : 1, vertical ? 1 : 0, t);
+            }
+        }
+        const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
+        t.write(rec, off, SPAN && wraps(t.st.flags, g.wrap), e);
+    }
+    t.st.max = t.mx;
+    p.state[r] = t.st;
+}
+
+// ------------------------------------------------------------ initialisers
+__global__ void init_site_nodes_kernel(uint64_t total, uint32_t *nodes) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        nodes[i] = kEmpty;
+}
+
+__global__ void init_torus_cells_kernel(uint64_t total, uint32_t word, uint4 *cells) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        cells[i] = make_uint4(word, 0u, 0u, 0u);
+}
+
+// bond model: N clusters of one node; site model: nothing occupied
+__global__ void init_lattice_state_kernel(int32_t n_runs, uint32_t N, uint32_t site, RunState *state) {
+    const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_runs) return;
+    RunState s;
+    const uint32_t c = site ? 0u : N;
+    s.t2 = c; s.t3 = c; s.t4_lo = c; s.t4_hi = 0;
+    s.t0 = c; s.max = site ? 0u : 1u; s.flags = 0u; s.pad = 0;
+    state[r] = s;
+}
+
+unsigned grid_for(uint64_t total) {
+    uint64_t blocks = (total + 255) / 256;
+    if (blocks > 152ull * 64) blocks = 152ull * 64;
+    return (unsigned)(blocks ? blocks : 1);
+}
+
+template <int KIND, int PERM>
+void launch_site_k(const UfParams &p, bool span, int block, cudaStream_t s) {
+    dim3 grid((p.n_runs + block - 1) / block);
+    if (span) site_window_kernel<KIND, PERM, true><<<grid, block, 0, s>>>(p);
+    else site_window_kernel<KIND, PERM, false><<<grid, block, 0, s>>>(p);
+}
+
+template <bool SITE, int PERM>
+void launch_torus_k(const UfParams &p, bool span, int block, cudaStream_t s) {
+    dim3 grid((p.n_runs + block - 1) / block);
+    if (span) torus_window_kernel<SITE, PERM, true><<<grid, block, 0, s>>>(p);
+    else torus_window_kernel<SITE, PERM, false><<<grid, block, 0, s>>>(p);
+}
+
+template <int PERM>
+void launch_lattice_perm(const UfParams &p, bool span, int block, cudaStream_t s) {
+    if (p.g.kind == NZ_GRAPH_TORUS2D) {
+        if (p.g.site) launch_torus_k<true, PERM>(p, span, block, s);
+        else launch_torus_k<false, PERM>(p, span, block, s);
+    } else if (p.g.kind == NZ_GRAPH_GRID2D) {
+        launch_site_k<NZ_GRAPH_GRID2D, PERM>(p, span, block, s);
+    } else {
+        launch_site_k<NZ_GRAPH_CHAIN1D, PERM>(p, span, block, s);
+    }
+}
+
+}  // namespace
+
+bool lattice_extension(const GraphDev &g) { return g.site || g.kind == NZ_GRAPH_TORUS2D; }
+
+void launch_init_lattice_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,
+                              cudaStream_t s) {
+    const uint64_t total = (uint64_t)n_runs * g.N;
+    if (g.kind == NZ_GRAPH_TORUS2D)
+        init_torus_cells_kernel<<<grid_for(total), 256, 0, s>>>(total, g.site ? kEmpty : make_root(1u, 0u),
+                                                                 reinterpret_cast<uint4 *>(nodes));
+    else
+        init_site_nodes_kernel<<<grid_for(total), 256, 0, s>>>(total, nodes);
+    init_lattice_state_kernel<<<(n_runs + 255) / 256, 256, 0, s>>>(n_runs, g.N, g.site, state);
+}
+
+void launch_lattice_window(const UfParams &p, int perm_mode, bool span, int block, cudaStream_t s) {
+    if (perm_mode == NZ_PERM_PHILOX) launch_lattice_perm<NZ_PERM_PHILOX>(p, span, block, s);
+    else launch_lattice_perm<NZ_PERM_GIVEN>(p, span, block, s);
+}
+
+}  // namespace nz

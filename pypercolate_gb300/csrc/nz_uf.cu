@@ -280,7 +280,7 @@ __global__ void pack_rows_kernel(NzRecords rec, int32_t run, uint32_t N, uint32_
         if (spanning) { d[8] = (ms & kSpanBit) ? 1 : 0; o = 9; }
         put_bytes(d + o, mx, 4);
         put_bytes(d + o + 4, rec.m0[off], 8);
-        put_bytes(d + o + 12, (uint64_t)(N - mx), 8);
+        put_bytes(d + o + 12, (uint64_t)((rec.site ? n : N) - mx), 8);
         put_bytes(d + o + 20, rec.m2[off], 8);
         put_bytes(d + o + 28, rec.m3[off], 8);
         put_bytes(d + o + 36, rec.m4_lo[off], 8);
@@ -299,6 +299,7 @@ static void launch_init_nodes_k(const GraphDev &g, int32_t n_runs, uint32_t *nod
 
 void launch_init_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,
                       uint32_t *flag_scratch, cudaStream_t s) {
+    if (lattice_extension(g)) { launch_init_lattice_runs(g, n_runs, nodes, state, s); return; }
     if (g.kind == NZ_GRAPH_GRID2D) launch_init_nodes_k<NZ_GRAPH_GRID2D>(g, n_runs, nodes, s);
     else if (g.kind == NZ_GRAPH_CHAIN1D) launch_init_nodes_k<NZ_GRAPH_CHAIN1D>(g, n_runs, nodes, s);
     else launch_init_nodes_k<NZ_GRAPH_EDGES>(g, n_runs, nodes, s);
@@ -325,6 +326,7 @@ static void launch_uf_kind(const UfParams &p, int perm_mode, bool span, int bloc
 }
 
 void launch_uf_window(const UfParams &p, int perm_mode, bool span, int block, cudaStream_t s) {
+    if (lattice_extension(p.g)) { launch_lattice_window(p, perm_mode, span, block, s); return; }
     if (p.g.kind == NZ_GRAPH_GRID2D) launch_uf_kind<NZ_GRAPH_GRID2D>(p, perm_mode, span, block, s);
     else if (p.g.kind == NZ_GRAPH_CHAIN1D) launch_uf_kind<NZ_GRAPH_CHAIN1D>(p, perm_mode, span, block, s);
     else launch_uf_kind<NZ_GRAPH_EDGES>(p, perm_mode, span, block, s);

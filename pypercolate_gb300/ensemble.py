@@ -20,13 +20,31 @@ import numpy as np
 from . import _native as nat
 from . import hpc
 
-_KINDS = {'grid': nat.GRAPH_GRID2D, 'chain': nat.GRAPH_CHAIN1D}
+_KINDS = {'grid': nat.GRAPH_GRID2D, 'chain': nat.GRAPH_CHAIN1D, 'torus': nat.GRAPH_TORUS2D}
+
+
+def lattice_kind(kind, model='bond', wrap='either'):
+    """NZ_GRAPH_* code with its model / wrapping flags."""
+    if kind not in _KINDS:
+        raise ValueError('unknown lattice %r' % (kind,))
+    if model not in ('bond', 'site'):
+        raise ValueError("model must be 'bond' or 'site'")
+    if wrap not in nat.WRAP:
+        raise ValueError('wrap must be one of %s' % sorted(nat.WRAP))
+    if wrap != 'either' and kind != 'torus':
+        raise ValueError('a wrapping criterion needs the torus')
+    return _KINDS[kind] | (nat.MODEL_SITE if model == 'site' else 0) | nat.WRAP[wrap]
 
 
 class Ensemble:
     """Running canonical / microcanonical averages of one lattice.
 
-    kind      'grid' (spanning_2d_grid(length)) or 'chain' (spanning_1d_chain)
+    kind      'grid' (spanning_2d_grid(length)), 'chain' (spanning_1d_chain) or
+              'torus' (length x length periodic square lattice, whose
+              "spanning" curves are wrapping probabilities, criterion `wrap`:
+              'either', 'x', 'y' or 'both' directions)
+    model     'bond' (the reference's model) or 'site' percolation; for site
+              percolation M = N steps, and p is the site occupation probability
     ps        occupation probabilities of the canonical curves
     precision 'fp32' (FP32 products, FP64 accumulation over row chunks) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
@@ -34,11 +52,13 @@ class Ensemble:
     """
 
     def __init__(self, kind='grid', length=16, ps=None, spanning=True, precision='fp32',
-                 micro=True, window=0, cutoff=80.0):
+                 micro=True, window=0, cutoff=80.0, model='bond', wrap='either'):
         torch = nat.torch_cuda()
         self.kind = kind
+        self.model = model
+        self.wrap = wrap
         self.length = int(length)
-        self.spec = hpc.GraphSpec(_KINDS[kind], self.length)
+        self.spec = hpc.GraphSpec(lattice_kind(kind, model, wrap), self.length)
         self.N, self.M = self.spec.N, self.spec.M
         self.ps = np.atleast_1d(np.asarray(ps if ps is not None else np.linspace(0, 1, 101),
                                            dtype=np.float64))
@@ -62,6 +82,7 @@ class Ensemble:
                 m2=torch.zeros(6 * rows, dtype=torch.float64, device='cuda'))
         self._ws = None
         self._ws_runs = 0
+        self.ledger = []  # (key, first run id, number of runs) of every batch added
 
     # ------------------------------------------------------------------
     def _micro_struct(self):
@@ -92,6 +113,84 @@ class Ensemble:
                              nat.ptr(self.count), nat.ptr(self.mean), nat.ptr(self.m2),
                              micro, nat.stream_handle(stream))
         nat.check(st, 'nz_ensemble')
+        self.ledger.append((int(key), int(run0), n_runs))
+        return self
+
+    # ------------------------------------------------------------------ state
+    def state_meta(self):
+        return {'kind': self.kind, 'model': self.model, 'wrap': self.wrap,
+                'length': self.length, 'N': self.N, 'M': self.M,
+                'spanning': self.spanning, 'precision': {0: 'fp64', 1: 'fp32'}[self.precision],
+                'window': self.window, 'cutoff': self.cutoff, 'micro': self.micro is not None}
+
+    def state(self):
+        """The accumulated state as host arrays (the checkpoint contents of
+        pypercolate_gb300.store)."""
+        from . import store
+        st = {'meta': self.state_meta(), 'ps': self.ps.copy(),
+              'count': self.count.cpu().numpy().copy(), 'mean': self.mean.cpu().numpy().copy(),
+              'm2': self.m2.cpu().numpy().copy(), 'ledger': store.ledger_array(self.ledger),
+              'micro': None}
+        if self.micro is not None:
+            st['micro'] = {k: v.cpu().numpy().copy() for k, v in self.micro.items()}
+        return st
+
+    @classmethod
+    def from_state(cls, state, window=None):
+        """An ensemble holding exactly the accumulated state `state`."""
+        from . import store
+        store.check_state(state)
+        meta = state['meta']
+        ens = cls(meta['kind'], meta['length'], state['ps'], spanning=meta['spanning'],
+                  precision=meta['precision'], micro=meta['micro'],
+                  window=meta['window'] if window is None else window, cutoff=meta['cutoff'],
+                  model=meta['model'], wrap=meta['wrap'])
+        if (ens.N, ens.M) != (meta['N'], meta['M']):
+            raise ValueError('state describes N=%s, M=%s; the lattice has N=%d, M=%d'
+                             % (meta['N'], meta['M'], ens.N, ens.M))
+        torch = nat.torch_cuda()
+        ens.count.copy_(torch.from_numpy(np.asarray(state['count'], np.int64).reshape(1)))
+        ens.mean.copy_(torch.from_numpy(np.asarray(state['mean'], np.float64)))
+        ens.m2.copy_(torch.from_numpy(np.asarray(state['m2'], np.float64)))
+        if ens.micro is not None:
+            for k, v in ens.micro.items():
+                v.copy_(torch.from_numpy(np.ascontiguousarray(state['micro'][k])))
+        ens.ledger = [tuple(int(x) for x in row) for row in store.ledger_array(state['ledger'])]
+        return ens
+
+    def save(self, path):
+        """Atomic checkpoint of the accumulated state (a .npz file)."""
+        from . import store
+        store.save_state(path, self.state())
+
+    @classmethod
+    def load(cls, path, window=None):
+        from . import store
+        return cls.from_state(store.load_state(path), window=window)
+
+    def merge(self, other):
+        """Adds the runs of another ensemble of the same lattice and p grid
+        (another GPU's shard, another process's checkpoint) to this one, on
+        the device: canonical (count, mean, M2) and the microcanonical
+        accumulators merge pairwise, exact sums add.  Raises ValueError if
+        the two share a run (same key and run id)."""
+        from . import store
+        if isinstance(other, dict):
+            other = Ensemble.from_state(other)
+        if not store.compatible(self.state_meta(), other.state_meta(), self.ps, other.ps):
+            raise ValueError('ensembles differ in lattice, p grid or arithmetic')
+        ledger = store.ledger_array(list(self.ledger) + list(other.ledger))
+        if store.ledger_overlaps(ledger):
+            raise ValueError('ensembles share runs; merging would count them twice')
+        lib = nat.lib_handle()
+        s = nat.stream_handle()
+        if self.micro is not None:
+            nat.check(lib.nz_micro_merge(self._micro_struct(), other._micro_struct(), self.M, s),
+                      'nz_micro_merge')
+        nat.check(lib.nz_canonical_merge(nat.ptr(self.count), nat.ptr(self.mean), nat.ptr(self.m2),
+                                         nat.ptr(other.count), nat.ptr(other.mean),
+                                         nat.ptr(other.m2), 7 * self.P, s), 'nz_canonical_merge')
+        self.ledger = list(self.ledger) + list(other.ledger)
         return self
 
     # ------------------------------------------------------------------

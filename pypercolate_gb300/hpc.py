@@ -94,20 +94,26 @@ class GraphSpec:
     order (so that ``edge`` indices match the reference's)."""
 
     def __init__(self, kind, length=0, num_nodes=0, num_edges=0, eu=None, ev=None, side=None):
-        self.kind = kind
+        self.kind = int(kind)  # NZ_GRAPH_* with the NZ_MODEL_SITE / NZ_WRAP_* flags
+        self.base = self.kind & nat.KIND_MASK
+        self.site = bool(self.kind & nat.MODEL_SITE)
         self.length = int(length)
         self.eu, self.ev, self.side = eu, ev, side
         self._dev = None
-        if kind == nat.GRAPH_GRID2D:
+        if self.base == nat.GRAPH_GRID2D:
             self.N, self.M = self.length ** 2, 2 * self.length * (self.length - 1)
-        elif kind == nat.GRAPH_CHAIN1D:
+        elif self.base == nat.GRAPH_CHAIN1D:
             self.N, self.M = self.length, self.length - 1
+        elif self.base == nat.GRAPH_TORUS2D:
+            self.N, self.M = self.length ** 2, 2 * self.length ** 2
         else:
             self.N, self.M = int(num_nodes), int(num_edges)
+        if self.site:
+            self.M = self.N  # one step per site
 
     def struct(self):
         """NzGraph descriptor (uploads an explicit edge list once)."""
-        if self.kind != nat.GRAPH_EDGES:
+        if self.base != nat.GRAPH_EDGES:
             return nat.make_graph(self.kind, self.length)
         if self._dev is None:
             self._dev = (nat.to_device(self.eu.astype(np.uint32)),
@@ -230,7 +236,7 @@ def _run_microcanonical(spec, spanning, seeds=None, rng='numpy', key=0, run0=0, 
     else:
         mode = nat.PERM_MT19937
         n_runs = len(seeds)
-    rec = nat.Records(spec.M + 1, n_runs, with_edge=with_edge)
+    rec = nat.Records(spec.M + 1, n_runs, with_edge=with_edge, site=getattr(spec, 'site', False))
     ws_bytes = lib.nz_microcanonical_workspace_bytes(g, n_runs, mode)
     ws = nat.device_empty(ws_bytes)
     d_perm = d_words = d_len = None

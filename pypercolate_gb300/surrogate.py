@@ -1,7 +1,10 @@
 """Learned surrogate of the canonical curves, judged by Monte Carlo.
 
 An MLP (4 hidden layers of width 128, GELU) maps (p, 1/L, lattice type
-one-hot [square 2D, chain 1D]) to (spanning probability, percolation
+one-hot [square 2D, chain 1D]) -- plus the finite-size-scaling variable
+asinh((p - p_c) L^(1/nu)) derived from them (p_c = 1/2, nu = 4/3 for bond
+percolation on the square lattice; p_c = 1, nu = 1 for the chain), on which
+the curves of different L collapse -- to (spanning probability, percolation
 strength, log-susceptibility), where susceptibility = m2 / N (the mean size
 of the non-largest clusters, sum' s^2 / N).  It is trained with the
 library's own BF16/FP32 forward, backward and Adam kernels (libnzgb300
@@ -17,18 +20,24 @@ import numpy as np
 
 from . import _native as nat
 
-WIDTHS = (4, 128, 128, 128, 128, 3)
+WIDTHS = (5, 128, 128, 128, 128, 3)
 OUTPUTS = ('spanning_probability', 'percolation_strength', 'log_susceptibility')
 KIND_2D, KIND_CHAIN = 'grid', 'chain'
 
 
+# (p_c, 1/nu) of the two lattice families
+SCALING = {KIND_2D: (0.5, 0.75), KIND_CHAIN: (1.0, 1.0)}
+
+
 def features(ps, L, kind):
-    """Input rows (p, 1/L, is_square_2d, is_chain_1d)."""
+    """Input rows (p, 1/L, is_square_2d, is_chain_1d, asinh((p - p_c) L^(1/nu)))."""
     ps = np.asarray(ps, dtype=np.float64)
-    out = np.zeros((ps.size, 4), dtype=np.float32)
+    out = np.zeros((ps.size, WIDTHS[0]), dtype=np.float32)
     out[:, 0] = ps
     out[:, 1] = 1.0 / float(L)
     out[:, 2 if kind == KIND_2D else 3] = 1.0
+    p_c, inv_nu = SCALING[kind]
+    out[:, 4] = np.arcsinh((ps - p_c) * float(L) ** inv_nu)
     return out
 
 
@@ -101,8 +110,8 @@ class MLP:
         nat.check(lib.nz_mlp_params_to_bf16(nat.ptr(self.params), self.count,
                                             nat.ptr(self.params_bf16), nat.stream_handle()),
                   'nz_mlp_params_to_bf16')
-        self.x_mean = np.zeros(4, np.float32)
-        self.x_std = np.ones(4, np.float32)
+        self.x_mean = np.zeros(int(widths[0]), np.float32)
+        self.x_std = np.ones(int(widths[0]), np.float32)
         self.y_mean = np.zeros(3, np.float32)
         self.y_std = np.ones(3, np.float32)
         self._buf = {}
@@ -123,7 +132,7 @@ class MLP:
         return self._buf[batch]
 
     def forward_device(self, x):
-        """x: device float32 [batch, 4] (already standardised) -> device y."""
+        """x: device float32 [batch, widths[0]] (already standardised) -> device y."""
         batch = x.shape[0]
         b = self._buffers(batch)
         nat.check(nat.lib_handle().nz_mlp_forward(

@@ -51,6 +51,35 @@ def test_host_only_entry_points(lib):
     assert L.nz_binomial_band_cap(130560, 80.0) > 2 * 12 * 181
 
 
+def test_lattice_extension_kinds(lib):
+    """Kind flags: torus sizes, site model (one step per site), rejected mixes."""
+    from pypercolate_gb300 import _native as nat
+    from pypercolate_gb300.ensemble import lattice_kind
+    L = nat.lib_handle()
+    size = lambda kind, n: nat.graph_size(nat.make_graph(kind, n))  # noqa: E731
+    assert size(nat.GRAPH_TORUS2D, 5) == (25, 50)
+    assert size(nat.GRAPH_TORUS2D | nat.WRAP['both'], 1) == (1, 2)
+    assert size(nat.GRAPH_GRID2D | nat.MODEL_SITE, 5) == (25, 25)
+    assert size(nat.GRAPH_CHAIN1D | nat.MODEL_SITE, 7) == (7, 7)
+    assert size(nat.GRAPH_TORUS2D | nat.MODEL_SITE | nat.WRAP['x'], 4) == (16, 16)
+    for bad in (nat.GRAPH_GRID2D | nat.WRAP['x'], nat.GRAPH_CHAIN1D | nat.WRAP['y'],
+                nat.GRAPH_TORUS2D | 0x800, nat.GRAPH_GRID2D | 0x1000):
+        with pytest.raises(ValueError):
+            size(bad, 4)
+    with pytest.raises(ValueError):  # site percolation needs an implicit lattice
+        nat.graph_size(nat.make_graph(nat.GRAPH_EDGES | nat.MODEL_SITE, 0, 3, 2))
+    with pytest.raises(nat.NzError):
+        size(nat.GRAPH_TORUS2D, 1449)  # 1449^2 > 2^21 nodes
+    # torus cells are 16 bytes per site
+    g = nat.make_graph(nat.GRAPH_TORUS2D, 64)
+    assert L.nz_microcanonical_workspace_bytes(g, 10, nat.PERM_PHILOX) >= 10 * 4096 * 16
+    assert lattice_kind('torus', 'site', 'both') == nat.GRAPH_TORUS2D | nat.MODEL_SITE | 0x600
+    with pytest.raises(ValueError):
+        lattice_kind('grid', 'bond', 'x')
+    with pytest.raises(ValueError):
+        lattice_kind('torus', 'sites')
+
+
 def test_dtypes_match_reference_layout():
     from pypercolate_gb300 import hpc
     assert np.dtype(hpc.microcanonical_statistics_dtype(True)).itemsize == 53
@@ -137,3 +166,21 @@ def test_log_uniform_thresholds():
     assert abs(np.mean(L <= 64) - 0.5) < 0.01
     assert abs(np.mean(L <= 22) - 0.25) < 0.02
     assert np.array_equal(log_uniform_thresholds(5, 5), [0])
+
+
+def test_surrogate_features():
+    """Host-side inputs of the surrogate: (p, 1/L, one-hot, scaling variable)."""
+    from pypercolate_gb300 import surrogate as S
+    ps = np.array([0.0, 0.5, 0.6, 1.0])
+    x = S.features(ps, 16, 'grid')
+    assert x.shape == (4, S.WIDTHS[0]) and x.dtype == np.float32
+    np.testing.assert_allclose(x[:, 0], ps)
+    np.testing.assert_allclose(x[:, 1], 1 / 16)
+    assert np.all(x[:, 2] == 1) and np.all(x[:, 3] == 0)
+    np.testing.assert_allclose(x[:, 4], np.arcsinh((ps - 0.5) * 8.0), rtol=1e-6)  # 16^(3/4) = 8
+    # the same (p - p_c) L^(1/nu) at two sizes gives the same scaling input
+    a = S.features([0.5 + 0.1 / 8], 16, 'grid')[0, 4]
+    b = S.features([0.5 + 0.1 / 64], 256, 'grid')[0, 4]
+    assert abs(a - b) < 1e-6
+    c = S.features([1.0 - 3.0 / 1024], 1024, 'chain')
+    assert c[0, 3] == 1 and abs(c[0, 4] - np.arcsinh(-3.0)) < 1e-6

@@ -152,7 +152,8 @@ def test_exact_records_vs_oracle(gpu, oracle, kind, L, R):
 
 
 def test_exact_beyond_uint64_L724(gpu, oracle):
-    """At L=724 sum' s^4 exceeds 2**64 in these runs: the high word is exact."""
+    """At L=724 sum' s^4 exceeds 2**64 in some runs (run 0 of key 5 here):
+    the high word is exact."""
     from pypercolate_gb300 import hpc
     spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, 724)
     rec = hpc._run_microcanonical(spec, True, rng='philox', key=5, run0=0, n_runs=3,
@@ -166,7 +167,7 @@ def test_exact_beyond_uint64_L724(gpu, oracle):
         assert np.array_equal(h['m4_lo'][:, r], ref['moments_u64'][:, 4])
         assert np.array_equal(h['m3'][:, r], ref['moments_u64'][:, 3])
         assert np.array_equal(h['max_span'][:, r] & 0x7fffffff, ref['max'])
-    assert wrapped == 3
+    assert wrapped >= 1
 
 
 def test_edge_cases(gpu):

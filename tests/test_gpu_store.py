@@ -1,0 +1,89 @@
+"""Checkpoint / resume and merging of GPU ensembles: a resumed job and a
+merge of shards give the same bits as one uninterrupted ensemble."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def gpu():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip('no CUDA device')
+    from pypercolate_gb300 import _native as nat
+    nat.lib_handle()
+    return nat
+
+
+PS = np.linspace(0.3, 0.7, 41)
+
+
+def make():
+    from pypercolate_gb300.ensemble import Ensemble
+    return Ensemble('grid', 24, PS, precision='fp32', micro=True)
+
+
+def bits(ens):
+    st = ens.state()
+    out = [st['count'], st['mean'], st['m2']] + [st['micro'][k] for k in sorted(st['micro'])]
+    return [np.asarray(a).tobytes() for a in out]
+
+
+def test_resume_is_bit_identical(gpu, tmp_path):
+    from pypercolate_gb300 import store
+    ref = make()
+    for run0 in (0, 300, 600):
+        ref.run(min(300, 700 - run0), key=5, run0=run0)
+    path = str(tmp_path / 'ck.npz')
+    # three "jobs", each allowed one batch, then one that finds nothing to do
+    for expect_done in (False, False, True):
+        ens, done = store.run_checkpointed(path, make, 700, 300, key=5, max_batches=1)
+        assert done == expect_done
+    ens, done = store.run_checkpointed(path, make, 700, 300, key=5, max_batches=1)
+    assert done and ens.ledger == ref.ledger
+    assert bits(ens) == bits(ref)
+    assert bits(type(ens).load(path)) == bits(ref)
+    np.testing.assert_array_equal(ens.canonical_averages(), ref.canonical_averages())
+    m_ens, m_ref = ens.microcanonical_averages(), ref.microcanonical_averages()
+    for k in m_ref:
+        np.testing.assert_array_equal(m_ens[k], m_ref[k])
+    # a checkpoint of another lattice is refused, not merged into
+    from pypercolate_gb300.ensemble import Ensemble
+    with pytest.raises(ValueError, match='different ensemble'):
+        store.run_checkpointed(path, lambda: Ensemble('grid', 25, PS, micro=True), 700, 300, key=5)
+    assert os.listdir(tmp_path) == ['ck.npz']
+
+
+def test_merge_of_shards_equals_one_ensemble(gpu):
+    whole = make()
+    whole.run(400, key=9, run0=0)
+    whole.run(250, key=9, run0=400)
+    a = make().run(400, key=9, run0=0)
+    b = make().run(250, key=9, run0=400)
+    a.merge(b)
+    assert bits(a) == bits(whole)
+    # merging a saved state (dict) works the same way
+    c = make().run(400, key=9, run0=0)
+    c.merge(b.state())
+    assert bits(c) == bits(whole)
+    with pytest.raises(ValueError, match='twice'):
+        a.merge(make().run(10, key=9, run0=640))
+    from pypercolate_gb300.ensemble import Ensemble
+    with pytest.raises(ValueError, match='differ'):
+        a.merge(Ensemble('grid', 24, PS[:-1], micro=True))
+
+
+def test_merge_matches_bond_reduce_of_rows(gpu):
+    """The device merge agrees with bond_reduce on the reference's rows."""
+    from pypercolate_gb300 import hpc
+    a = make().run(300, key=2, run0=0)
+    b = make().run(500, key=2, run0=300)
+    rows = hpc.bond_reduce(a.canonical_averages(), b.canonical_averages())
+    a.merge(b)
+    got = a.canonical_averages()
+    assert np.all(got['number_of_runs'] == 800)
+    for f in got.dtype.names[1:]:
+        np.testing.assert_allclose(got[f], rows[f], rtol=1e-12, atol=1e-12)

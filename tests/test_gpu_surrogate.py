@@ -24,7 +24,7 @@ def test_forward_and_gradients_match_fp64_oracle(gpu):
     rng = np.random.default_rng(3)
     model = MLP(seed=5)
     B = 96
-    x = rng.normal(size=(B, 4)).astype(np.float32)
+    x = rng.normal(size=(B, WIDTHS[0])).astype(np.float32)
     t = rng.normal(size=(B, 3)).astype(np.float32)
     w = rng.uniform(0.5, 2.0, size=(B, 3)).astype(np.float32)
     dx, dt, dw = (torch.from_numpy(a).cuda() for a in (x, t, w))
@@ -63,7 +63,7 @@ def test_adam_matches_reference_update(gpu):
 def test_training_fits_a_smooth_function(gpu):
     from pypercolate_gb300.surrogate import MLP
     rng = np.random.default_rng(0)
-    X = rng.uniform(0, 1, size=(20000, 4)).astype(np.float32)
+    X = rng.uniform(0, 1, size=(20000, 5)).astype(np.float32)
     Y = np.column_stack([np.tanh(8 * (X[:, 0] - 0.5)), X[:, 1] ** 2, np.sin(3 * X[:, 2])])
     model = MLP(seed=2)
     trace = model.fit(X, Y, steps=400, batch=4096, lr=1e-3, log_every=100)

@@ -202,3 +202,77 @@ def test_classic_microcanonical_averages(oracle):
         np.testing.assert_allclose(mlo / N, z[pre + 'max_cluster_size_ci'][:, 0],
                                    rtol=1e-9)
         np.testing.assert_allclose(mom.mean(0).T / N, z[pre + 'moments'], rtol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# brute-force census (oracle/nz_census.c): the checker of site percolation and
+# of wrapping on the torus, pinned here by reproducing the pinned restatement
+# of the reference's bond path
+@pytest.mark.parametrize('kind,L', [('grid', 2), ('grid', 5), ('grid', 16), ('chain', 2),
+                                    ('chain', 40)])
+def test_census_reproduces_bond_oracle(oracle, kind, L):
+    for run in range(4):
+        N, M = oracle.census_size(kind, L, False)
+        perm = oracle.philox_permutation(77, run, M)
+        c = oracle.lattice_census(kind, L, perm)
+        r = oracle.lattice_run(0 if kind == 'grid' else 1, L, perm)
+        lo, hi = r['moments_u64'], r['moments_hi']
+        np.testing.assert_array_equal(c['max_span'] & 0x7FFFFFFF, r['max'])
+        np.testing.assert_array_equal((c['max_span'] >> 31).astype(bool), r['span'])
+        np.testing.assert_array_equal(c['m0'], lo[:, 0])
+        for k, name in ((2, 'm2'), (3, 'm3'), (4, 'm4_lo')):
+            np.testing.assert_array_equal(c[name], lo[:, k])
+        np.testing.assert_array_equal(c['m4_hi'].astype(np.uint64), hi[:, 4])
+
+
+def test_census_known_configurations(oracle):
+    # torus: the bonds of row 0 close a horizontal loop at the L-th bond
+    c = oracle.lattice_census('torus', 4, np.arange(32), wrap='x')
+    assert list(c['max_span'][:6] >> 31) == [0, 0, 0, 0, 1, 1]
+    c = oracle.lattice_census('torus', 4, np.arange(32), wrap='y')
+    # vertical bonds start at index 16; column 0's loop closes at bond 16 + 12
+    flags = c['max_span'] >> 31
+    assert flags[28] == 0 and flags[29] == 1
+    both = oracle.lattice_census('torus', 4, np.arange(32), wrap='both')['max_span'] >> 31
+    assert np.array_equal(both, flags)  # x wraps first here, so both == y
+    # everything open / occupied: one cluster of N, nothing else
+    for kind, L, site in (('torus', 5, False), ('torus', 5, True), ('grid', 6, True),
+                          ('chain', 9, True)):
+        N, S = oracle.census_size(kind, L, site)
+        c = oracle.lattice_census(kind, L, np.arange(S), site=site)
+        assert (c['max_span'][-1] & 0x7FFFFFFF) == N and c['m0'][-1] == 0 and c['m2'][-1] == 0
+        assert c['max_span'][-1] >> 31 == 1
+    # site model: nothing occupied at n = 0
+    c = oracle.lattice_census('grid', 3, np.arange(9), site=True)
+    assert c['max_span'][0] == 0 and c['m0'][0] == 0 and c['m2'][0] == 0
+    # one site on a 1 x 1 torus is its own neighbour in both directions
+    c = oracle.lattice_census('torus', 1, np.arange(1), site=True, wrap='both')
+    assert list(c['max_span'] >> 31) == [0, 1]
+
+
+def test_philox_permutation_is_statistically_uniform(oracle):
+    """The keyed Feistel permutation behaves like a uniform random one where
+    an affine-like round function fails: on a 32 x 32 torus (M = 2048 bonds,
+    the first N horizontal) the share of horizontal bonds among the first M/2
+    has the hypergeometric spread; position and value are independent
+    (16 x 16 chi-square); consecutive elements are uncorrelated."""
+    L = 32
+    N, M = L * L, 2 * L * L
+    runs = 400
+    P = np.stack([oracle.philox_permutation(99, r, M) for r in range(runs)]).astype(np.int64)
+    for r in range(0, runs, 50):
+        assert np.array_equal(np.sort(P[r]), np.arange(M))
+    share = (P[:, :M // 2] < N).mean(1)
+    sd_hyper = np.sqrt(M / 16.0 / (M - 1) * M) / (M / 2)  # = 0.0111
+    assert abs(share.mean() - 0.5) < 4 * sd_hyper / np.sqrt(runs)
+    assert 0.8 < share.std() / sd_hyper < 1.25
+    pos = np.broadcast_to(np.arange(M) * 16 // M, P.shape).ravel()
+    table = np.bincount(pos * 16 + (P * 16 // M).ravel(), minlength=256).astype(float)
+    expected = P.size / 256.0
+    chi2 = ((table - expected) ** 2 / expected).sum()
+    assert chi2 < 225 + 5 * np.sqrt(2 * 225)
+    step = np.abs(np.diff(P, axis=1)).mean()
+    assert abs(step / (M / 3.0) - 1) < 0.01   # E|U - V| = M/3 for independent uniforms
+    # and the permutation depends on the key and the run id
+    assert not np.array_equal(P[0], P[1])
+    assert not np.array_equal(oracle.philox_permutation(98, 0, M), P[0])

@@ -36,7 +36,8 @@ UF_BYTES_PER_ADD = 4 * 32 + 36
 # ncu capture of spanning_2d_grid(256), 12,288 runs, one 1,024-row window at
 # p ~ 0.5 (profiles/window_kernels_L256_12288_runs.md); a full launch's
 # traffic is this figure times the additions it makes
-UF_TRAFFIC_PER_ADD = 206.5
+UF_TRAFFIC_PER_ADD = 187.4
+UF_READ_PER_ADD = 90.8  # of which read (the scattered finds)
 
 
 def parse():
@@ -71,6 +72,34 @@ def peaks():
         d = json.load(open(path))
         return float(d['hbm_gbs']), 'measured'
     return 6800.0, 'fallback'
+
+
+def random_gather_rate(gib=16, k=1 << 28, reps=3):
+    """Random-access ceiling of this GPU's HBM: 4-byte gathers at uniformly
+    random positions of a `gib` GiB array (far larger than L2), each touching
+    its own 32-byte sector; returns sectors (gathers) per second, best of
+    `reps` (CUDA events).  The union-find's finds are such accesses."""
+    import torch
+    n = (gib << 30) // 4
+    a = torch.zeros(n, dtype=torch.int32, device='cuda')
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(7)
+    idx = torch.randint(0, n, (k,), device='cuda', generator=gen)
+    out = torch.empty(k, dtype=torch.int32, device='cuda')
+    torch.index_select(a, 0, idx, out=out)
+    best = None
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.index_select(a, 0, idx, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        best = t if best is None else min(best, t)
+    del a, idx, out
+    torch.cuda.empty_cache()
+    return k / best
 
 
 class ClockSampler:
@@ -377,6 +406,9 @@ def main():
     achieved = UF_BYTES_PER_ADD * adds_per_launch / uf_avg_s / 1e9
     peak, peak_kind = peaks()
     launches = {k: v[0] for k, v in prof.items()}
+    # second ceiling for the union-find: HBM's rate of scattered sector reads
+    gather_rate = random_gather_rate()
+    uf_adds_per_s = adds_per_launch / uf_avg_s
     kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 1, 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
@@ -474,7 +506,14 @@ def main():
                                        'launch by its additions',
                      'kernel': 'uf_window_kernel', 'peak_source': peak_kind,
                      'bytes_per_addition': UF_BYTES_PER_ADD,
-                     'avg_launch_ms': uf_avg_s * 1e3},
+                     'avg_launch_ms': uf_avg_s * 1e3,
+                     'random_access': {
+                         'gather_sectors_per_s': gather_rate,
+                         'uf_read_sectors_per_s': uf_adds_per_s * UF_READ_PER_ADD / 32.0,
+                         'frac': uf_adds_per_s * UF_READ_PER_ADD / 32.0 / gather_rate,
+                         'note': 'ceiling = 4-B torch.index_select gathers at random positions of '
+                                 'a 16 GiB array; union-find sector reads from the measured '
+                                 '%.1f B read per addition' % UF_READ_PER_ADD}},
         'kernel_ms_per_step': {k: v[1] / args.steps for k, v in prof.items()},
         'plain_gpu': plain,
         'batched_uneven': mix,

@@ -8,8 +8,9 @@
  *     "host"), never throws, and returns an NZ_* status code;
  *   - is stream-ordered on the `stream` argument (a cudaStream_t, NULL = the
  *     legacy default stream) and does not synchronise unless stated;
- *   - allocates nothing: the caller owns every buffer, including scratch,
- *     whose size the *_workspace_bytes functions report.
+ *   - allocates no device memory: the caller owns every buffer, including
+ *     scratch, whose size the *_workspace_bytes functions report (nz_ensemble
+ *     keeps CUDA stream and event handles of its own, see there).
  * Calls on one stream are serialised by the stream; concurrent calls on
  * different streams must not share output or workspace buffers.
  *
@@ -298,7 +299,13 @@ int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
  * -> banded canonical convolution at P probabilities -> pairwise merge.
  * Results are merged into (acc_count, acc_mean[P*7], acc_m2[P*7]) and, if
  * micro != NULL, into *micro.  conv_precision: 0 = FP64, 1 = FP32 with
- * FP64 chunk accumulation. */
+ * FP64 chunk accumulation.  The union-find runs on `stream`; the reductions
+ * and the convolution of each window of records run on a second stream of
+ * the library's (one per concurrent call and device, created on first use
+ * and kept), overlapping the union-find of the next window, and are joined
+ * back into `stream` before the call returns: work enqueued on `stream`
+ * afterwards sees the results.  Make a first call before capturing `stream`
+ * into a CUDA graph. */
 size_t nz_ensemble_workspace_bytes(const NzGraph *graph, int32_t n_runs,
                                    int32_t P, int32_t window);
 int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,

@@ -81,7 +81,7 @@ constexpr uint32_t kRecordBytes = 4 + 4 + 8 + 8 + 8 + 4;  // planes without edge
 // Workspace of the microcanonical entry point.
 size_t micro_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t perm_mode, uint32_t **nodes,
                     RunState **state, uint32_t **flag, uint32_t **perms) {
-    *nodes = c.take<uint32_t>((size_t)n_runs * g.N * node_words(g));
+    *nodes = c.take<uint32_t>((size_t)n_runs * g.slots);
     *state = c.take<RunState>((size_t)n_runs);
     *flag = c.take<uint32_t>(4);
     *perms = perm_mode == NZ_PERM_MT19937 ? c.take<uint32_t>((size_t)n_runs * (g.M ? g.M : 1)) : nullptr;
@@ -260,6 +260,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
                                     int32_t spanning, const uint32_t *band_lo, const uint32_t *band_len,
                                     const double *weights, int32_t cap, int32_t P, double *out, void *stream) {
     if (!rec || !band_lo || !band_len || !weights || !out || n_runs <= 0 || P <= 0) return NZ_ERR_INVALID;
+    if (!conv_grid_fits(n_runs, P)) return NZ_ERR_TOO_LARGE;
     cudaStream_t s = as_stream(stream);
     if (cudaMemsetAsync(out, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess) return NZ_ERR_CUDA;
     ConvParams p;
@@ -370,7 +371,7 @@ struct EnsembleLayout {
     uint32_t *nodes;
     RunState *state;
     uint32_t *flag;
-    NzRecords rec;
+    NzRecords rec[2];  // double-buffered record windows
     uint32_t *band_lo, *band_len;
     double *w64;
     float *w32;
@@ -383,9 +384,54 @@ struct EnsembleLayout {
 
 constexpr double kDefaultCutoff = 80.0;
 
+// A second stream per device on which nz_ensemble runs the consumers of each
+// record window (micro reductions, convolution, final reduction) while the
+// union-find fills the next window on the caller's stream, with the events
+// that order the two.  Slots are created on first use and kept for the life
+// of the process; a call holds one for as long as it enqueues work, so
+// concurrent calls never share events.
+struct AuxSlot {
+    int device;
+    cudaStream_t s2;
+    cudaEvent_t fork, join, produced[2], consumed[2];
+    bool busy;
+};
+
+struct AuxPool {
+    std::mutex mu;
+    std::vector<AuxSlot *> slots;
+};
+AuxPool g_aux;
+
+AuxSlot *aux_checkout() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_aux.mu);
+    for (AuxSlot *a : g_aux.slots)
+        if (!a->busy && a->device == dev) { a->busy = true; return a; }
+    AuxSlot *a = new AuxSlot();
+    a->device = dev;
+    bool ok = cudaStreamCreateWithFlags(&a->s2, cudaStreamNonBlocking) == cudaSuccess;
+    cudaEvent_t *evs[6] = {&a->fork, &a->join, &a->produced[0], &a->produced[1], &a->consumed[0], &a->consumed[1]};
+    for (cudaEvent_t *e : evs) ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) { delete a; return nullptr; }  // (a failed creation leaks at most the handles made)
+    a->busy = true;
+    g_aux.slots.push_back(a);
+    return a;
+}
+
+struct AuxGuard {
+    AuxSlot *a;
+    ~AuxGuard() {
+        if (!a) return;
+        std::lock_guard<std::mutex> lk(g_aux.mu);
+        a->busy = false;
+    }
+};
+
 int32_t pick_window(uint32_t M, int32_t n_runs, int32_t window) {
     if (window > 0) return window > (int32_t)(M + 1) ? (int32_t)(M + 1) : window;
-    // records of one window at most ~8 GiB
+    // records of one window at most ~8 GiB (two windows in flight)
     double w = 8.0 * (1ull << 30) / ((double)n_runs * kRecordBytes);
     if (w < 256) w = 256;
     if (w > M + 1) w = M + 1;
@@ -396,19 +442,22 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
                        EnsembleLayout &L) {
     L.window = pick_window(g.M, n_runs, window);
     L.cap = nz_binomial_band_cap(g.M, cutoff);
-    L.nodes = c.take<uint32_t>((size_t)n_runs * g.N * node_words(g));
+    L.nodes = c.take<uint32_t>((size_t)n_runs * g.slots);
     L.state = c.take<RunState>((size_t)n_runs);
     L.flag = c.take<uint32_t>(4);
     const size_t plane = (size_t)L.window * n_runs;
-    L.rec.max_span = c.take<uint32_t>(plane);
-    L.rec.m0 = c.take<uint32_t>(plane);
-    L.rec.m2 = c.take<uint64_t>(plane);
-    L.rec.m3 = c.take<uint64_t>(plane);
-    L.rec.m4_lo = c.take<uint64_t>(plane);
-    L.rec.m4_hi = c.take<uint32_t>(plane);
-    L.rec.edge = nullptr;
-    L.rec.run_stride = n_runs;
-    L.rec.site = (int32_t)g.site;
+    for (int b = 0; b < 2; ++b) {
+        NzRecords &r = L.rec[b];
+        r.max_span = c.take<uint32_t>(plane);
+        r.m0 = c.take<uint32_t>(plane);
+        r.m2 = c.take<uint64_t>(plane);
+        r.m3 = c.take<uint64_t>(plane);
+        r.m4_lo = c.take<uint64_t>(plane);
+        r.m4_hi = c.take<uint32_t>(plane);
+        r.edge = nullptr;
+        r.run_stride = n_runs;
+        r.site = (int32_t)g.site;
+    }
     L.band_lo = c.take<uint32_t>(P);
     L.band_len = c.take<uint32_t>(P);
     L.w64 = c.take<double>((size_t)P * L.cap);
@@ -443,6 +492,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     int st = graph_size(*graph, N, M);
     if (st) return st;
     if (graph->kind == NZ_GRAPH_EDGES) return NZ_ERR_INVALID;  // lattices only on the fast path
+    if (!conv_grid_fits(n_runs, P)) return NZ_ERR_TOO_LARGE;
     if (micro && (!micro->count || !micro->span_count || !micro->sum_lo || !micro->sum_hi || !micro->m2))
         return NZ_ERR_INVALID;
     GraphDev g = make_graph_dev(*graph, N, M);
@@ -461,6 +511,13 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
             return NZ_ERR_CUDA;
     }
 
+    AuxGuard aux{aux_checkout()};
+    if (!aux.a) return NZ_ERR_CUDA;
+    cudaStream_t s2 = aux.a->s2;
+    // fork: the consumer stream starts after the set-up above
+    if (cudaEventRecord(aux.a->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, aux.a->fork, 0) != cudaSuccess)
+        return NZ_ERR_CUDA;
+
     UfParams up;
     up.g = g;
     up.n_runs = n_runs;
@@ -469,9 +526,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     up.key = key;
     up.run0 = run0;
     up.perms = nullptr;
-    up.rec = L.rec;
     ConvParams cp;
-    cp.rec = L.rec;
     cp.N = N;
     cp.n_runs = n_runs;
     cp.spanning = spanning;
@@ -484,36 +539,54 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.acc = L.stats;
     MicroParams mp;
     if (micro) {
-        mp.rec = L.rec;
         mp.N = N;
         mp.n_runs = n_runs;
         mp.acc = *micro;
         mp.M = M;
         mp.count_before = micro->count;
     }
-    for (uint32_t w0 = 0; w0 <= M; w0 += (uint32_t)L.window) {
+    // Window k: the union-find fills record buffer k % 2 on `s` while the
+    // micro reductions and the convolution of window k - 1 read the other
+    // buffer on s2.  The union-find of window k waits until the consumers of
+    // window k - 2 (same buffer) are done; the consumers of window k wait for
+    // its union-find.  Node words and run state live on `s` only, the
+    // accumulators on s2 only.
+    int k = 0;
+    for (uint32_t w0 = 0; w0 <= M; w0 += (uint32_t)L.window, ++k) {
         const uint32_t w1 = (w0 + (uint32_t)L.window > M + 1) ? M + 1 : w0 + (uint32_t)L.window;
+        const int b = k & 1;
+        if (k >= 2 && cudaStreamWaitEvent(s, aux.a->consumed[b], 0) != cudaSuccess) return NZ_ERR_CUDA;
+        up.rec = L.rec[b];
         up.n_begin = w0; up.n_end = w1;
         {
             ProfScope prof(NZ_PROF_UNION_FIND, s);
             launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, 128, s);  // 64 and 256 per CTA: same time
         }
+        if (cudaEventRecord(aux.a->produced[b], s) != cudaSuccess ||
+            cudaStreamWaitEvent(s2, aux.a->produced[b], 0) != cudaSuccess)
+            return NZ_ERR_CUDA;
         if (micro) {
-            ProfScope prof(NZ_PROF_MICRO, s);
+            ProfScope prof(NZ_PROF_MICRO, s2);
+            mp.rec = L.rec[b];
             mp.n_begin = w0; mp.n_end = w1;
-            launch_micro_window(mp, s);
+            launch_micro_window(mp, s2);
         }
         {
-            ProfScope prof(NZ_PROF_CONV, s);
+            ProfScope prof(NZ_PROF_CONV, s2);
+            cp.rec = L.rec[b];
             cp.n_begin = w0; cp.n_end = w1;
-            launch_conv_window(cp, conv_precision, s);
+            launch_conv_window(cp, conv_precision, s2);
         }
+        if (cudaEventRecord(aux.a->consumed[b], s2) != cudaSuccess) return NZ_ERR_CUDA;
     }
     {
-        ProfScope prof(NZ_PROF_REDUCE, s);
-        if (micro) launch_micro_count(micro->count, n_runs, s);
-        launch_reduce_runs(L.stats, n_runs, P, acc_count, acc_mean, acc_m2, L.part, L.slices, s);
+        ProfScope prof(NZ_PROF_REDUCE, s2);
+        if (micro) launch_micro_count(micro->count, n_runs, s2);
+        launch_reduce_runs(L.stats, n_runs, P, acc_count, acc_mean, acc_m2, L.part, L.slices, s2);
     }
+    // join: `s` continues after everything on s2
+    if (cudaEventRecord(aux.a->join, s2) != cudaSuccess || cudaStreamWaitEvent(s, aux.a->join, 0) != cudaSuccess)
+        return NZ_ERR_CUDA;
     return check_launch();
 }
 

@@ -258,6 +258,10 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
 constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
 constexpr int kConvPT = NZ_CONV_PT;    // probabilities per CTA
 constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before an FP64 flush
+#ifndef NZ_CONV_BATCH
+#define NZ_CONV_BATCH 8
+#endif
+constexpr int kConvBatch = NZ_CONV_BATCH;  // record loads in flight per thread
 
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
 // kConvPT canonical values of its run for one statistic over the window's
@@ -273,12 +277,28 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
 #pragma unroll
     for (int j = 0; j < kConvPT; ++j) part[j] = 0;
     const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
-    for (uint32_t i = 0; i < cn; ++i) {
+    // m1 = (sites in clusters) - max: N for bond records, n for site records
+    auto value = [&](uint32_t i) -> wtype {
         const size_t off = base + (size_t)i * p.rec.run_stride;
-        // m1 = (sites in clusters) - max: N for bond records, n for site records
         const uint32_t held = (S == 3 && SITE) ? c0 + i : p.N;
-        const wtype q = PRECISION == 0 ? (wtype)record_value<S>(p.rec, off, held)
-                                       : (wtype)record_value_f<S>(p.rec, off, held);
+        return PRECISION == 0 ? (wtype)record_value<S>(p.rec, off, held)
+                              : (wtype)record_value_f<S>(p.rec, off, held);
+    };
+    // the records of kConvBatch rows are loaded before their products so that
+    // that many loads are in flight per thread; each accumulator still adds
+    // the rows in increasing order
+    uint32_t i = 0;
+    for (; i + kConvBatch <= cn; i += kConvBatch) {
+        wtype q[kConvBatch];
+#pragma unroll
+        for (int b = 0; b < kConvBatch; ++b) q[b] = value(i + b);
+#pragma unroll
+        for (int b = 0; b < kConvBatch; ++b)
+#pragma unroll
+            for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i + b][j], q[b], part[j]);
+    }
+    for (; i < cn; ++i) {
+        const wtype q = value(i);
 #pragma unroll
         for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
     }
@@ -356,8 +376,15 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     }
 }
 
+bool conv_grid_fits(int32_t n_runs, int32_t P) {
+    // grid.y (p tiles) is limited to 65535
+    return n_runs > 0 && P > 0 && (P + kConvPT - 1) / kConvPT <= 65535;
+}
+
 void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
+    // (run tiles, p tiles, statistics); launching the p tiles of one run tile
+    // back to back (for L2 reuse of its records) measured slower
     dim3 grid((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 7);
     // the record model is a template parameter: a run-time test in the row
     // loop cost 17 % of the kernel's time

@@ -134,12 +134,29 @@ struct GraphDev {
     uint32_t site;        // NZ_MODEL_SITE given: M = N steps occupy sites
     uint32_t wrap;        // torus: NZ_WRAP_* >> 9 (0 either, 1 x, 2 y, 3 both)
     uint32_t L, N, M;
+    uint32_t slots;       // union-find words per run (>= N: layout padding, torus cells)
+    uint32_t tile_cols;   // grid: 4 x 2 site blocks per block row, (L+3)/4
     uint32_t row_edges;   // grid: (L-1)*(2L-1) edges in rows 0..L-2
     uint32_t two_l_m1;    // grid: 2L-1
     float inv_two_l_m1;   // grid: 1/(2L-1)
     const uint32_t *eu, *ev;
     const uint8_t *side;
 };
+
+// Bond percolation on the square grid keeps its node words in blocks of
+// 4 x 2 sites, one block per 32-byte sector (block rows of (L+3)/4 blocks),
+// instead of row-major: both ends of a random bond then share a sector 5/8 of
+// the time instead of 7/16, and small clusters span fewer sectors.  Node
+// words hold these slot indices as parents; the records do not depend on the
+// layout.
+#ifndef NZ_GRID_TILED
+#define NZ_GRID_TILED 1
+#endif
+constexpr bool kGridTiled = NZ_GRID_TILED != 0;
+
+__host__ __device__ __forceinline__ uint32_t grid_slot(uint32_t tile_cols, uint32_t r, uint32_t c) {
+    return ((r >> 1) * tile_cols + (c >> 2)) * 8u + ((r & 1u) << 2) + (c & 3u);
+}
 
 inline int graph_size_base(const NzGraph &g, int kind, uint32_t &N, uint32_t &M);
 
@@ -196,11 +213,16 @@ inline GraphDev make_graph_dev(const NzGraph &g, uint32_t N, uint32_t M) {
     d.row_edges = 0;
     d.two_l_m1 = 1;
     d.inv_two_l_m1 = 1.0f;
+    d.tile_cols = 0;
+    d.slots = N;
     if (d.kind == NZ_GRAPH_GRID2D) {
         d.two_l_m1 = 2u * g.length - 1u;
         d.row_edges = (g.length - 1u) * d.two_l_m1;
         d.inv_two_l_m1 = 1.0f / (float)d.two_l_m1;
+        d.tile_cols = (g.length + 3u) >> 2;
+        if (kGridTiled && !d.site) d.slots = ((g.length + 1u) >> 1) * d.tile_cols * 8u;
     }
+    if (d.kind == NZ_GRAPH_TORUS2D) d.slots = 4u * N;
     d.eu = g.edge_u;
     d.ev = g.edge_v;
     d.side = g.node_side;
@@ -236,6 +258,40 @@ __device__ __forceinline__ void decode_edge(const GraphDev &g, uint32_t e, uint3
     }
 }
 
+// Ends of edge e as slots of the run's node array (grid_slot on the tiled
+// square grid, the node ids otherwise).
+template <int KIND>
+__device__ __forceinline__ void decode_edge_slots(const GraphDev &g, uint32_t e, uint32_t &u, uint32_t &v) {
+    if (KIND == NZ_GRAPH_GRID2D && kGridTiled) {
+        uint32_t r, c;
+        bool right;
+        if (e < g.row_edges) {
+            r = div_small(e, g.two_l_m1, g.inv_two_l_m1);
+            const uint32_t w = e - r * g.two_l_m1;
+            c = w >> 1;
+            right = (w & 1u) != 0;
+        } else {
+            r = g.L - 1u;
+            c = e - g.row_edges;
+            right = true;
+        }
+        u = grid_slot(g.tile_cols, r, c);
+        v = right ? grid_slot(g.tile_cols, r, c + 1u) : grid_slot(g.tile_cols, r + 1u, c);
+    } else {
+        decode_edge<KIND>(g, e, u, v);
+    }
+}
+
+// slot of node i (see decode_edge_slots)
+template <int KIND>
+__device__ __forceinline__ uint32_t node_slot(const GraphDev &g, uint32_t i) {
+    if (KIND == NZ_GRAPH_GRID2D && kGridTiled) {
+        const uint32_t r = i / g.L;
+        return grid_slot(g.tile_cols, r, i - r * g.L);
+    }
+    return i;
+}
+
 template <int KIND>
 __device__ __forceinline__ uint32_t node_sides(const GraphDev &g, uint32_t i) {
     if (KIND == NZ_GRAPH_GRID2D) {
@@ -264,10 +320,5 @@ constexpr uint32_t kFlagCorrupt = 4u;   // a find exceeded the depth bound (neve
 constexpr uint32_t kFlagWrapX = 8u;     // torus: a cluster wraps along x
 constexpr uint32_t kFlagWrapY = 16u;    // torus: a cluster wraps along y
 
-// 32-bit words of union-find state per node: the torus kernels keep the
-// node word and the displacement (dx, dy) to the parent in one 16-byte cell
-__host__ __device__ __forceinline__ uint32_t node_words(const GraphDev &g) {
-    return g.kind == NZ_GRAPH_TORUS2D ? 4u : 1u;
-}
 
 }  // namespace nz

@@ -13,7 +13,7 @@ namespace nz {
 struct UfParams {
     GraphDev g;
     int32_t n_runs;
-    uint32_t *nodes;        // [n_runs][N * node_words(g)]
+    uint32_t *nodes;        // [n_runs][g.slots]
     RunState *state;        // [n_runs]
     uint32_t n_begin;       // rows emitted: [n_begin, n_end)
     uint32_t n_end;
@@ -61,6 +61,7 @@ struct ConvParams {
     const float *w32;        // [P][cap] (FP32 path)
     double *acc;             // [n_runs][P][7], accumulated (+=)
 };
+bool conv_grid_fits(int32_t n_runs, int32_t P);  // grid of launch_conv_window within CUDA's limits
 void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s);
 void launch_weights_to_f32(const double *w64, float *w32, size_t count, cudaStream_t s);
 // part: scratch [slices][P*7][3] doubles

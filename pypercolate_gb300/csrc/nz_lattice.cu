@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) site_window_kernel(UfParams p) {
     const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.n_runs) return;
     const GraphDev &g = p.g;
-    uint32_t *node = p.nodes + (size_t)r * g.N;
+    uint32_t *node = p.nodes + (size_t)r * g.slots;  // slots == N: site lattices are not tiled
     Tally t;
     t.load(p.state[r]);
     FeistelPerm fp;

@@ -180,6 +180,7 @@ __device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L,
                         const MixRec &out, size_t rec_base) {
     GraphDev g;
     g.kind = KIND; g.site = 0; g.wrap = 0; g.L = L; g.N = N; g.M = M;
+    g.slots = N; g.tile_cols = 0;  // row-major node ids (decode_edge, not decode_edge_slots)
     g.two_l_m1 = KIND == NZ_GRAPH_GRID2D ? 2u * L - 1u : 1u;
     g.row_edges = KIND == NZ_GRAPH_GRID2D ? (L - 1u) * g.two_l_m1 : 0u;
     g.inv_two_l_m1 = 1.0f / (float)g.two_l_m1;

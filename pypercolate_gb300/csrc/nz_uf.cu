@@ -37,8 +37,9 @@ __global__ void init_nodes_kernel(GraphDev g, int32_t n_runs, uint32_t *nodes) {
     const uint64_t total = (uint64_t)n_runs * g.N;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t k = (uint32_t)(i % g.N);
-        nodes[i] = make_root(1u, node_sides<KIND>(g, k));
+        const uint64_t r = i / g.N;
+        const uint32_t k = (uint32_t)(i - r * g.N);
+        nodes[r * g.slots + node_slot<KIND>(g, k)] = make_root(1u, node_sides<KIND>(g, k));
     }
 }
 
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
     const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.n_runs) return;
     const GraphDev &g = p.g;
-    uint32_t *node = p.nodes + (size_t)r * g.N;
+    uint32_t *node = p.nodes + (size_t)r * g.slots;
     RunState st = p.state[r];
 
     FeistelPerm fp;
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
             if (PERM != NZ_PERM_PHILOX && e >= g.M) {
                 u = v = 0;  // caller-supplied index out of range: no bond added
             } else {
-                decode_edge<KIND>(g, e, u, v);
+                decode_edge_slots<KIND>(g, e, u, v);
                 if (KIND == NZ_GRAPH_EDGES && (u >= g.N || v >= g.N)) u = v = 0;  // invalid edge list
             }
             // two interleaved finds with path splitting

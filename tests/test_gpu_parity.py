@@ -151,6 +151,25 @@ def test_exact_records_vs_oracle(gpu, oracle, kind, L, R):
         assert np.array_equal(h['edge'][1:, r], ref['edge'][1:])
 
 
+def test_full_occupancy_launch_matches_oracle(gpu, oracle):
+    """One union-find launch with 16,384 runs of spanning_2d_grid(128) (every
+    SM full of resident warps, 19 GB of records): sampled runs across the
+    launch equal the oracle row for row."""
+    from pypercolate_gb300 import hpc
+    spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, 128)
+    R = 16384
+    rec = hpc._run_microcanonical(spec, True, rng='philox', key=77, run0=5000, n_runs=R,
+                                  with_edge=False)
+    for r in (0, 1, 31, 4097, 9999, R - 1):
+        ref = oracle.lattice_run(0, 128, oracle.philox_permutation(77, 5000 + r, spec.M))
+        col = {k: getattr(rec, k)[r::R].cpu().numpy() for k in ('max_span', 'm2', 'm4_lo')}
+        assert np.array_equal(col['max_span'].view(np.uint32) & 0x7fffffff, ref['max']), r
+        assert np.array_equal((col['max_span'].view(np.uint32) >> 31).astype(bool), ref['span']), r
+        assert np.array_equal(col['m2'].view(np.uint64), ref['moments_u64'][:, 2]), r
+        assert np.array_equal(col['m4_lo'].view(np.uint64), ref['moments_u64'][:, 4]), r
+    del rec
+
+
 def test_exact_beyond_uint64_L724(gpu, oracle):
     """At L=724 sum' s^4 exceeds 2**64 in some runs (run 0 of key 5 here):
     the high word is exact."""

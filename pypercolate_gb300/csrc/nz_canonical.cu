@@ -803,27 +803,51 @@ void launch_bond_reduce(const uint8_t *a, const uint8_t *b, int32_t P, int32_t s
 // finalized_canonical_averages_dtype (hpc.py:705-749):
 //   n u4, p f8, alpha f8, [pp_mean, pp_std, pp_ci 2*f8], strength_mean, strength_std,
 //   strength_ci 2*f8, moments_mean 5*f8, moments_std 5*f8, moments_ci 5*2*f8
-__device__ void t_interval(double conf, double df, double loc, double scale, double &lo, double &hi) {
-    // scipy.stats.t.interval: ppf((1 - conf)/2), ppf((1 + conf)/2); NaN unless
+// Student-t quantiles ppf((1 - conf)/2, df) and ppf((1 + conf)/2, df) for
+// the rows of a block: threads 0 and 1 evaluate them once for df0 (the df of
+// the block's first row) and share them; a row with another df evaluates its
+// own.  Every thread of the block must call this (it synchronises).
+struct TPair { double lo, hi; };
+
+__device__ TPair t_pair_block(double conf, double df0, double df, bool active) {
+    __shared__ double s_q[2];
+    if (threadIdx.x < 2)
+        s_q[threadIdx.x] = student_t_quantile(threadIdx.x == 0 ? (1.0 - conf) / 2.0 : (1.0 + conf) / 2.0, df0);
+    __syncthreads();
+    TPair r;
+    if (df == df0) { r.lo = s_q[0]; r.hi = s_q[1]; }
+    else if (active) {
+        r.lo = student_t_quantile((1.0 - conf) / 2.0, df);
+        r.hi = student_t_quantile((1.0 + conf) / 2.0, df);
+    } else { r.lo = r.hi = NAN; }
+    return r;
+}
+
+__device__ void t_interval(const TPair &q, double df, double loc, double scale, double &lo, double &hi) {
+    // scipy.stats.t.interval: loc + scale * ppf((1 -+ conf)/2); NaN unless
     // scale > 0 and df > 0.
     if (!(scale > 0.0) || !(df > 0.0) || isnan(loc)) { lo = NAN; hi = NAN; return; }
-    const double qa = (1.0 - conf) / 2.0, qb = (1.0 + conf) / 2.0;
-    lo = loc + scale * student_t_quantile(qa, df);
-    hi = loc + scale * student_t_quantile(qb, df);
+    lo = loc + scale * q.lo;
+    hi = loc + scale * q.hi;
 }
 
 __global__ void finalize_kernel(const uint8_t *avg, int32_t P, int32_t spanning, double N, const double *ps,
                                 double alpha, uint8_t *out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P) return;
     const int nst = spanning ? 7 : 6;
-    const uint8_t *a = avg + (size_t)i * (4 + nst * 16);
-    uint8_t *o = out + (size_t)i * (spanning ? 244 : 212);
-    const uint32_t nu = *reinterpret_cast<const uint32_t *>(a);
-    const double n = (double)nu;
-    const double nm1 = (double)(uint32_t)(nu - 1u);  // numpy uint32 arithmetic
-    const double sqrt_n = sqrt(n);
+    const size_t in_row = 4 + nst * 16;
     const double conf = 1.0 - alpha;
+    // numpy uint32 arithmetic: n - 1 wraps for n = 0
+    const uint32_t nu0 = *reinterpret_cast<const uint32_t *>(avg + (size_t)blockIdx.x * blockDim.x * in_row);
+    const uint32_t nu_i = i < P ? *reinterpret_cast<const uint32_t *>(avg + (size_t)i * in_row) : nu0;
+    const TPair tq = t_pair_block(conf, (double)(uint32_t)(nu0 - 1u), (double)(uint32_t)(nu_i - 1u), i < P);
+    if (i >= P) return;
+    const uint8_t *a = avg + (size_t)i * in_row;
+    uint8_t *o = out + (size_t)i * (spanning ? 244 : 212);
+    const uint32_t nu = nu_i;
+    const double n = (double)nu;
+    const double nm1 = (double)(uint32_t)(nu - 1u);
+    const double sqrt_n = sqrt(n);
     *reinterpret_cast<uint32_t *>(o) = nu;
     st_f64(o + 4, ps[i]);
     st_f64(o + 12, alpha);
@@ -834,7 +858,7 @@ __global__ void finalize_kernel(const uint8_t *avg, int32_t P, int32_t spanning,
         st_f64(pm, mu);
         st_f64(pstd, sd);
         double lo, hi;
-        t_interval(conf, nm1, mu, sd / sqrt_n, lo, hi);
+        t_interval(tq, nm1, mu, sd / sqrt_n, lo, hi);
         st_f64(pci, lo);
         st_f64(pci + 8, hi);
     };
@@ -864,8 +888,10 @@ void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, 
 __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
                                       int32_t normalize, double *out) {
     const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n > M) return;
     const double R = (double)*acc.count;
+    // every row has R runs: one pair of t quantiles per block
+    const TPair tq = t_pair_block(1.0 - alpha, R - 1.0, R - 1.0, n <= M);
+    if (n > M) return;
     double *o = out + (size_t)n * 21;
     if (spanning) {
         const double k = (double)acc.span_count[n];
@@ -883,10 +909,9 @@ __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, 
         const double sd = R > 1.0 ? sqrt(m2 / (R - 1.0)) : NAN;
         double lo = mean, hi = mean;
         if (sd > 0.0) {
-            const double conf = 1.0 - alpha;
             const double sc = sd / sqrt(R);
-            lo = mean + sc * student_t_quantile((1.0 - conf) / 2.0, R - 1.0);
-            hi = mean + sc * student_t_quantile((1.0 + conf) / 2.0, R - 1.0);
+            lo = mean + sc * tq.lo;
+            hi = mean + sc * tq.hi;
         }
         const double scale = normalize ? (double)N : 1.0;
         o[3 + 3 * j] = mean / scale;

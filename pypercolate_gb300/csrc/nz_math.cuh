@@ -110,11 +110,19 @@ NZ_HD inline double student_t_quantile(double q, double v) {
     const double tail = q > 0.5 ? 1.0 - q : q;  // upper-tail probability of |t|
     if (v == 1.0) return sgn * tan(M_PI * (0.5 - tail));
     if (v == 2.0) { const double p2 = 2.0 * tail; return sgn * sqrt(2.0 / (p2 * (2.0 - p2)) - 2.0); }
-    // Cornish-Fisher start about the normal quantile
+    // Cornish-Fisher expansion about the normal quantile (Abramowitz & Stegun
+    // 26.7.5).  With four terms it is the quantile to double precision for
+    // v >= 1e4 (<= 1e-15 relative against scipy for tails 1e-8 .. 0.5), and
+    // the Newton iteration below, whose incomplete-beta continued fraction
+    // needs hundreds of terms at large v, is skipped; below it is the start.
     const double z = -nz_normal_quantile(tail);
     const double z2 = z * z;
     double t = z + (z2 + 1.0) * z / (4.0 * v) + ((5.0 * z2 + 16.0) * z2 + 3.0) * z / (96.0 * v * v) +
                (((3.0 * z2 + 19.0) * z2 + 17.0) * z2 - 15.0) * z / (384.0 * v * v * v);
+    if (v >= 1e4 && isfinite(z)) {
+        t += ((((79.0 * z2 + 776.0) * z2 + 1482.0) * z2 - 1920.0) * z2 - 945.0) * z / (92160.0 * v * v * v * v);
+        return sgn * t;
+    }
     if (!(t > 0.0) || !isfinite(t)) t = z > 0.0 ? z : 1.0;
     // bracket [lo, hi] with tail(lo) >= target >= tail(hi)
     double lo = 0.0, hi = t;

@@ -28,7 +28,9 @@ def make():
 
 def bits(ens):
     st = ens.state()
-    out = [st['count'], st['mean'], st['m2']] + [st['micro'][k] for k in sorted(st['micro'])]
+    out = [st['count'], st['mean'], st['m2']]
+    if st['micro'] is not None:
+        out += [st['micro'][k] for k in sorted(st['micro'])]
     return [np.asarray(a).tobytes() for a in out]
 
 
@@ -87,3 +89,29 @@ def test_merge_matches_bond_reduce_of_rows(gpu):
     assert np.all(got['number_of_runs'] == 800)
     for f in got.dtype.names[1:]:
         np.testing.assert_allclose(got[f], rows[f], rtol=1e-12, atol=1e-12)
+
+
+def test_state_of_other_models_round_trips(gpu, tmp_path):
+    """Site percolation and torus wrapping ensembles (micro on and off) keep
+    their model in the checkpoint, resume and merge like bond ensembles."""
+    from pypercolate_gb300 import store
+    from pypercolate_gb300.ensemble import Ensemble
+    for kw in (dict(kind='torus', length=12, model='site', wrap='both', micro=True),
+               dict(kind='grid', length=10, model='site', micro=False),
+               dict(kind='torus', length=9, model='bond', wrap='x', micro=False)):
+        make = lambda: Ensemble(kw['kind'], kw['length'], PS, micro=kw['micro'],  # noqa: E731
+                                model=kw['model'], wrap=kw.get('wrap', 'either'))
+        whole = make().run(120, key=4, run0=0).run(80, key=4, run0=120)
+        path = str(tmp_path / ('%s_%s.npz' % (kw['kind'], kw['model'])))
+        ens, done = store.run_checkpointed(path, make, 200, 120, key=4, max_batches=1)
+        assert not done
+        ens, done = store.run_checkpointed(path, make, 200, 120, key=4)
+        assert done
+        assert bits(ens) == bits(whole)
+        loaded = Ensemble.load(path)
+        assert (loaded.model, loaded.wrap, loaded.kind) == (kw['model'], kw.get('wrap', 'either'),
+                                                           kw['kind'])
+        # a bond ensemble of the same lattice is a different ensemble
+        if kw['model'] == 'site':
+            with pytest.raises(ValueError):
+                loaded.merge(Ensemble(kw['kind'], kw['length'], PS, micro=kw['micro']))

@@ -409,7 +409,7 @@ def main():
     # second ceiling for the union-find: HBM's rate of scattered sector reads
     gather_rate = random_gather_rate()
     uf_adds_per_s = adds_per_launch / uf_avg_s
-    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 1, 'reduce': 4}
+    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 2, 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
     # plain GPU path (one lattice per launch): chunks of runs whose records for

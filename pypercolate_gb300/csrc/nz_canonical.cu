@@ -306,12 +306,57 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
     for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
 }
 
-// grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
-// kConvPT canonical values of its run for one statistic over the window's
-// rows, with the tile's weights staged in shared memory (zero outside each
-// p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
-// products summed in FP32 over kConvChunk rows, then added into FP64.
+// Statistics 0 (spanning), 1 (max) and 3 (m1 = held - max) all come from the
+// max_span plane: one pass loads each word once and feeds the three sets of
+// products (each accumulator adds the same values in the same order as a
+// pass per statistic would).
 template <int PRECISION, bool SITE>
+__device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
+                                              const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
+                                              double *acc0, double *acc1, double *acc3) {
+    using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
+    wtype p0[kConvPT], p1[kConvPT], p3[kConvPT];
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) p0[j] = p1[j] = p3[j] = 0;
+    const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
+    auto step = [&](uint32_t i, uint32_t ms) {
+        const uint32_t held = SITE ? c0 + i : p.N;
+        const uint32_t mx = ms & ~kSpanBit;
+        const wtype q0 = (ms & kSpanBit) ? (wtype)1 : (wtype)0;
+        const wtype q1 = (wtype)mx, q3 = (wtype)(held - mx);
+#pragma unroll
+        for (int j = 0; j < kConvPT; ++j) {
+            const wtype w = s_w[i][j];
+            p0[j] = fma(w, q0, p0[j]);  // (dropped at the end without a spanning statistic)
+            p1[j] = fma(w, q1, p1[j]);
+            p3[j] = fma(w, q3, p3[j]);
+        }
+    };
+    uint32_t i = 0;
+    for (; i + kConvBatch <= cn; i += kConvBatch) {
+        uint32_t ms[kConvBatch];
+#pragma unroll
+        for (int b = 0; b < kConvBatch; ++b) ms[b] = p.rec.max_span[base + (size_t)(i + b) * p.rec.run_stride];
+#pragma unroll
+        for (int b = 0; b < kConvBatch; ++b) step(i + b, ms[b]);
+    }
+    for (; i < cn; ++i) step(i, p.rec.max_span[base + (size_t)i * p.rec.run_stride]);
+#pragma unroll
+    for (int j = 0; j < kConvPT; ++j) {
+        acc0[j] += (double)p0[j];
+        acc1[j] += (double)p1[j];
+        acc3[j] += (double)p3[j];
+    }
+}
+
+// Each thread accumulates the kConvPT canonical values of its run over the
+// window's rows, with the tile's weights staged in shared memory (zero
+// outside each p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1:
+// FP32 products summed in FP32 over kConvChunk rows, then added into FP64.
+// MAXSET: grid (run tiles, p tiles, 1), statistics 0, 1 and 3 from the
+// max_span plane in one pass; otherwise grid (run tiles, p tiles, 4),
+// statistics 2, 4, 5, 6 (one per z).
+template <int PRECISION, bool SITE, bool MAXSET>
 __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     __shared__ wtype s_w[kConvChunk][kConvPT];
@@ -319,8 +364,8 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     __shared__ uint32_t s_range[2];
     const int r = blockIdx.x * kConvRuns + threadIdx.x;
     const int p0 = blockIdx.y * kConvPT;
-    const int s = blockIdx.z;
-    if (s == 0 && !p.spanning) return;
+    constexpr int kOther[4] = {2, 4, 5, 6};
+    const int s = MAXSET ? 1 : kOther[blockIdx.z];
     if (threadIdx.x < kConvPT) {
         const int pi = p0 + threadIdx.x;
         s_lo[threadIdx.x] = pi < p.P ? p.band_lo[pi] : 0u;
@@ -338,9 +383,13 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = s_range[0], nhi = s_range[1];
     if (nlo >= nhi) return;
-    double acc[kConvPT];
+    double acc[kConvPT], acc0[MAXSET ? kConvPT : 1], acc3[MAXSET ? kConvPT : 1];
 #pragma unroll
     for (int j = 0; j < kConvPT; ++j) acc[j] = 0.0;
+    if (MAXSET) {
+#pragma unroll
+        for (int j = 0; j < kConvPT; ++j) acc0[j] = acc3[j] = 0.0;
+    }
     for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
         const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
         __syncthreads();
@@ -356,14 +405,15 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
         }
         __syncthreads();
         if (r < p.n_runs) {
-            switch (s) {
-                case 0: conv_rows<PRECISION, 0, SITE>(p, c0, cn, r, s_w, acc); break;
-                case 1: conv_rows<PRECISION, 1, SITE>(p, c0, cn, r, s_w, acc); break;
-                case 2: conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc); break;
-                case 3: conv_rows<PRECISION, 3, SITE>(p, c0, cn, r, s_w, acc); break;
-                case 4: conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc); break;
-                case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
-                default: conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc); break;
+            if (MAXSET) {
+                conv_rows_max<PRECISION, SITE>(p, c0, cn, r, s_w, acc0, acc, acc3);
+            } else {
+                switch (s) {
+                    case 2: conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc); break;
+                    case 4: conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc); break;
+                    case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
+                    default: conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc); break;
+                }
             }
         }
     }
@@ -371,7 +421,13 @@ __global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
 #pragma unroll
         for (int j = 0; j < kConvPT; ++j) {
             const int pi = p0 + j;
-            if (pi < p.P) p.acc[((size_t)r * p.P + pi) * 7 + s] += acc[j];
+            if (pi >= p.P) continue;
+            double *o = p.acc + ((size_t)r * p.P + pi) * 7;
+            o[s] += acc[j];
+            if (MAXSET) {
+                if (p.spanning) o[0] += acc0[j];
+                o[3] += acc3[j];
+            }
         }
     }
 }
@@ -385,15 +441,26 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
     // (run tiles, p tiles, statistics); launching the p tiles of one run tile
     // back to back (for L2 reuse of its records) measured slower
-    dim3 grid((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 7);
+    dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
+    dim3 gother(gmax.x, gmax.y, 4);
     // the record model is a template parameter: a run-time test in the row
     // loop cost 17 % of the kernel's time
     if (p.rec.site) {
-        if (precision == 0) conv_window_kernel<0, true><<<grid, kConvRuns, 0, s>>>(p);
-        else conv_window_kernel<1, true><<<grid, kConvRuns, 0, s>>>(p);
+        if (precision == 0) {
+            conv_window_kernel<0, true, true><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, true, false><<<gother, kConvRuns, 0, s>>>(p);
+        } else {
+            conv_window_kernel<1, true, true><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, true, false><<<gother, kConvRuns, 0, s>>>(p);
+        }
     } else {
-        if (precision == 0) conv_window_kernel<0, false><<<grid, kConvRuns, 0, s>>>(p);
-        else conv_window_kernel<1, false><<<grid, kConvRuns, 0, s>>>(p);
+        if (precision == 0) {
+            conv_window_kernel<0, false, true><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, false, false><<<gother, kConvRuns, 0, s>>>(p);
+        } else {
+            conv_window_kernel<1, false, true><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, false, false><<<gother, kConvRuns, 0, s>>>(p);
+        }
     }
 }
 

@@ -59,8 +59,14 @@ __global__ void init_state_kernel(int32_t n_runs, uint32_t N, const uint32_t *in
 }
 
 // ------------------------------------------------------------ main kernel
+#ifndef NZ_UF_MAX_THREADS
+#define NZ_UF_MAX_THREADS 256
+#endif
+#ifndef NZ_UF_MIN_BLOCKS
+#define NZ_UF_MIN_BLOCKS 1
+#endif
 template <int KIND, int PERM, bool SPAN>
-__global__ void __launch_bounds__(256) uf_window_kernel(UfParams p) {
+__global__ void __launch_bounds__(NZ_UF_MAX_THREADS, NZ_UF_MIN_BLOCKS) uf_window_kernel(UfParams p) {
     const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.n_runs) return;
     const GraphDev &g = p.g;

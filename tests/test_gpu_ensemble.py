@@ -157,3 +157,21 @@ def test_finalized_ensemble(gpu):
     np.testing.assert_allclose(fin['percolation_strength_ci'][:, 0], lo, rtol=1e-10)
     np.testing.assert_allclose(fin['percolation_strength_ci'][:, 1], hi, rtol=1e-10)
     assert np.all(fin['p'] == ps)
+
+
+@pytest.mark.parametrize('L', [339, 340])
+def test_m4_high_plane_either_side_of_its_bound(gpu, oracle, L):
+    """Up to N = 115,000 sites the ensemble leaves out the m4 high-word
+    plane (sum' s^4 < 2^64 there); L = 339 (N = 114,921) runs without it,
+    L = 340 (N = 115,600) with it.  Both give the oracle's exact sums."""
+    from pypercolate_gb300.ensemble import Ensemble
+    R = 3
+    ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True)
+    ens.run(R, key=21, run0=0)
+    got = ens.micro_sums()
+    M = 2 * L * (L - 1)
+    m4 = np.zeros(M + 1, dtype=object)
+    for r in range(R):
+        run = oracle.lattice_run(0, L, oracle.philox_permutation(21, r, M))
+        m4 += run['moments_u64'][:, 4].astype(object) + run['moments_hi'][:, 4].astype(object) * (1 << 64)
+    assert (got['sums'][5] == m4).all()

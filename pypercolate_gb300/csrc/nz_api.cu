@@ -430,6 +430,23 @@ struct AuxGuard {
     }
 };
 
+// Joins the consumer stream back into the caller's stream on every way out
+// of nz_ensemble once the fork is enqueued, so that nothing the caller
+// enqueues afterwards (or a freed workspace) can race the consumers.
+struct JoinGuard {
+    cudaStream_t s, s2;
+    cudaEvent_t join;
+    bool armed;
+    int join_now() {
+        armed = false;
+        return cudaEventRecord(join, s2) == cudaSuccess && cudaStreamWaitEvent(s, join, 0) == cudaSuccess
+                   ? NZ_OK : NZ_ERR_CUDA;
+    }
+    ~JoinGuard() {
+        if (armed) join_now();
+    }
+};
+
 int32_t pick_window(uint32_t M, int32_t n_runs, int32_t window) {
     if (window > 0) return window > (int32_t)(M + 1) ? (int32_t)(M + 1) : window;
     // records of one window at most ~8 GiB (two windows in flight)
@@ -521,6 +538,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     // fork: the consumer stream starts after the set-up above
     if (cudaEventRecord(aux.a->fork, s) != cudaSuccess || cudaStreamWaitEvent(s2, aux.a->fork, 0) != cudaSuccess)
         return NZ_ERR_CUDA;
+    JoinGuard joiner{s, s2, aux.a->join, true};
 
     UfParams up;
     up.g = g;
@@ -589,8 +607,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         launch_reduce_runs(L.stats, n_runs, P, acc_count, acc_mean, acc_m2, L.part, L.slices, s2);
     }
     // join: `s` continues after everything on s2
-    if (cudaEventRecord(aux.a->join, s2) != cudaSuccess || cudaStreamWaitEvent(s, aux.a->join, 0) != cudaSuccess)
-        return NZ_ERR_CUDA;
+    if (joiner.join_now() != NZ_OK) return NZ_ERR_CUDA;
     return check_launch();
 }
 

@@ -59,8 +59,7 @@ __global__ void init_state_kernel(int32_t n_runs, uint32_t N, const uint32_t *in
 }
 
 // ------------------------------------------------------------ main kernel
-// 9 resident CTAs of 128 threads per SM: at most 56 registers (24 bytes of
-// spills).  In the ensemble pipeline the union-find shares the SMs with the
+// 9 resident CTAs of 128 threads per SM: at most 56 registers.  In the ensemble pipeline the union-find shares the SMs with the
 // convolution of the previous window; a smaller register footprint leaves the
 // convolution more warps: 1491 ms per 100,000-run L = 256 step against 1636
 // ms at 70 registers and 1515 ms at 48.
@@ -82,11 +81,7 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
     else perm = p.perms + (size_t)r * g.M;
 
     const NzRecords rec = p.rec;
-    // powers of the largest cluster size, recomputed only when it grows
     uint32_t mx = st.max;
-    uint64_t mx2 = (uint64_t)mx * mx;
-    uint64_t mx3 = mx2 * mx;
-    uint64_t mx4_lo = mx3 * mx, mx4_hi = __umul64hi(mx3, (uint64_t)mx);
     for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
         uint32_t e = 0;
         if (n > 0) {
@@ -131,18 +126,17 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
                 st.t3 += 3ull * ab * s;
                 const uint64_t q = 4ull * a * a + 6ull * ab + 4ull * b * b;
                 add128(st.t4_lo, st.t4_hi, ab * q, __umul64hi(ab, q));
-                if (s > mx) {
-                    mx = s;
-                    mx2 = (uint64_t)mx * mx;
-                    mx3 = mx2 * mx;
-                    mx4_lo = mx3 * mx;
-                    mx4_hi = __umul64hi(mx3, (uint64_t)mx);
-                }
+                if (s > mx) mx = s;
                 if (SPAN && (sides == 3u || (st.flags & kFlagInitBoth))) st.flags |= kFlagSpan;
             }
         }
         // row n: moments = T_k - max^k
         const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
+        // powers of the largest size, recomputed per row (a few integer
+        // multiplies) rather than kept live: at the 56-register cap the
+        // kernel then needs no spills
+        const uint64_t mx2 = (uint64_t)mx * mx, mx3 = mx2 * mx;
+        const uint64_t mx4_lo = mx3 * mx, mx4_hi = __umul64hi(mx3, (uint64_t)mx);
         if (rec.max_span) rec.max_span[off] = mx | ((SPAN && (st.flags & kFlagSpan)) ? kSpanBit : 0u);
         if (rec.m0) rec.m0[off] = st.t0 - 1u;
         if (rec.m2) rec.m2[off] = st.t2 - mx2;

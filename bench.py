@@ -61,6 +61,11 @@ def parse():
                     help='runs of the batched uneven workload (0: skip)')
     ap.add_argument('--study', default=None, choices=[None, 'precision', 'surrogate'],
                     help='precision: FP32 vs FP64 canonical curves at L=1024 (separate line)')
+    ap.add_argument('--lattice', default='grid', choices=['grid', 'torus'],
+                    help='main leg lattice: spanning_2d_grid or the periodic square lattice '
+                         '(wrapping in either direction); for profiling the extensions')
+    ap.add_argument('--model', default='bond', choices=['bond', 'site'],
+                    help='main leg percolation model (site: one step per site)')
     ap.add_argument('--l2-fetch', type=int, default=32,
                     help='L2 fetch granularity of this process (bytes; 0 = leave as is)')
     return ap.parse_args()
@@ -360,9 +365,13 @@ def main():
         nat.set_l2_fetch_granularity(args.l2_fetch)
     l2_fetch = nat.get_l2_fetch_granularity()
     ps = np.linspace(0.0, 1.0, args.P)
-    N, M = L * L, 2 * L * (L - 1)
-    ens = Ensemble('grid', L, ps, precision=args.precision, micro=not args.no_micro,
-                   window=args.window)
+    ens = Ensemble(args.lattice, L, ps, precision=args.precision, micro=not args.no_micro,
+                   window=args.window, model=args.model)
+    N, M = ens.N, ens.M  # M = number of steps (bonds, or sites for the site model)
+    default_leg = args.lattice == 'grid' and args.model == 'bond'
+    unit = 'bond additions/s' if args.model == 'bond' else 'site additions/s'
+    if not default_leg:  # the extensions are measured on their own lattice only
+        args.plain_runs = args.mix_runs = 0
     run_base = rank * 10 ** 9  # disjoint run ids per rank (weak scaling)
 
     def barrier():
@@ -475,7 +484,7 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
-        e = Ensemble('grid', L, h_ps.numpy(), precision=args.precision,
+        e = Ensemble(args.lattice, L, h_ps.numpy(), precision=args.precision, model=args.model,
                      micro=not args.no_micro, window=args.window)
         e._ws = ens._ws  # reuse the device workspace
         e.d_ps.copy_(h_ps, non_blocking=True)
@@ -487,14 +496,16 @@ def main():
     e2e_value = R * M * world / e2e_s
 
     line = {
-        'metric': 'bond additions/s', 'value': value, 'unit': 'bond additions/s',
+        'metric': unit, 'value': value, 'unit': unit,
         'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'int32 union-find, u64/u128 moments, %s convolution' % args.precision,
         'data': 'synthetic (Philox-4x32-10 keyed permutations, seed %d)' % KEY,
-        'config': {'workload': 'spanning_2d_grid(%d) batched ensemble: %d runs/step/GPU, '
+        'config': {'workload': '%s batched ensemble: %d runs/step/GPU, '
                                '%d uniform p in [0,1], fused micro reductions=%s'
-                               % (L, R, args.P, not args.no_micro),
+                               % ('spanning_2d_grid(%d)' % L if default_leg else
+                                  '%s %s percolation, L=%d' % (args.lattice, args.model, L),
+                                  R, args.P, not args.no_micro),
                    'L': L, 'N': N, 'M': M, 'runs_per_step': R, 'P': args.P,
                    'precision': args.precision, 'l2_fetch_bytes': l2_fetch,
                    'l2': 'inputs larger than L2 (%.1f GB of union-find state per step)'
@@ -520,14 +531,23 @@ def main():
         'batched_vs_plain': (value / world / plain['value']) if plain else None,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
-        'e2e': {'value': e2e_value, 'unit': 'bond additions/s', 'h2d_bytes_per_step': h2d,
+        'e2e': {'value': e2e_value, 'unit': unit, 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h},
     }
+    if not default_leg:
+        # the traffic figure and the CPU oracle pipeline are for the bond grid
+        line['roofline']['kernel'] = ('torus_window_kernel' if args.lattice == 'torus'
+                                      else 'site_window_kernel')
+        line['roofline']['traffic'] = None
+        line['roofline'].pop('random_access', None)
     if rank == 0:
-        try:
-            line['cpu_baseline'] = cpu_baseline(L, ps, args.cpu_sample)
-        except Exception as exc:  # the oracle is a measurement aid only
-            line['cpu_baseline'] = {'value': None, 'error': repr(exc)}
+        if default_leg:
+            try:
+                line['cpu_baseline'] = cpu_baseline(L, ps, args.cpu_sample)
+            except Exception as exc:  # the oracle is a measurement aid only
+                line['cpu_baseline'] = {'value': None, 'error': repr(exc)}
+        else:
+            line['cpu_baseline'] = None
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

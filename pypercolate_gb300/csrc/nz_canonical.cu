@@ -359,12 +359,12 @@ __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, 
 // MAXSET: grid (run tiles, p tiles, 1), statistics 0, 1 and 3 from the
 // max_span plane in one pass; otherwise grid (run tiles, p tiles, 4),
 // statistics 2, 4, 5, 6 (one per z).
-template <int PRECISION, bool SITE, bool MAXSET>
 #ifdef NZ_CONV_MIN_BLOCKS
 #define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns, NZ_CONV_MIN_BLOCKS)
 #else
 #define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns)
 #endif
+template <int PRECISION, bool SITE, bool MAXSET>
 __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     __shared__ wtype s_w[kConvChunk][kConvPT];

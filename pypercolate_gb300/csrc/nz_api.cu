@@ -627,7 +627,7 @@ int mix_validate(const NzMixSpec *spec, int32_t n_runs, int32_t threads) {
 
 size_t mix_layout(Carver &c, const NzMixSpec &sp, int32_t n_runs, int32_t T, MixLaunch &L) {
     const uint32_t n_classes = (sp.grid_max - sp.grid_min + 1) + (sp.chain_max - sp.chain_min + 1);
-    const uint64_t nmax = std::max<uint64_t>((uint64_t)sp.grid_max * sp.grid_max, sp.chain_max);
+    const uint64_t nmax = std::max<uint64_t>(grid_slots(sp.grid_max), sp.chain_max);  // node words
     const size_t F = (size_t)sp.checkpoints;
     L.cls = c.take<uint32_t>(n_runs);
     L.counts = c.take<uint32_t>(n_classes);

@@ -158,6 +158,11 @@ __host__ __device__ __forceinline__ uint32_t grid_slot(uint32_t tile_cols, uint3
     return ((r >> 1) * tile_cols + (c >> 2)) * 8u + ((r & 1u) << 2) + (c & 3u);
 }
 
+// node words of an L x L grid in that layout (>= L^2, non-decreasing in L)
+__host__ __device__ __forceinline__ uint32_t grid_slots(uint32_t L) {
+    return kGridTiled ? ((L + 1u) >> 1) * ((L + 3u) >> 2) * 8u : L * L;
+}
+
 inline int graph_size_base(const NzGraph &g, int kind, uint32_t &N, uint32_t &M);
 
 inline int graph_size(const NzGraph &g, uint32_t &N, uint32_t &M) {
@@ -220,7 +225,7 @@ inline GraphDev make_graph_dev(const NzGraph &g, uint32_t N, uint32_t M) {
         d.row_edges = (g.length - 1u) * d.two_l_m1;
         d.inv_two_l_m1 = 1.0f / (float)d.two_l_m1;
         d.tile_cols = (g.length + 3u) >> 2;
-        if (kGridTiled && !d.site) d.slots = ((g.length + 1u) >> 1) * d.tile_cols * 8u;
+        if (!d.site) d.slots = grid_slots(g.length);
     }
     if (d.kind == NZ_GRAPH_TORUS2D) d.slots = 4u * N;
     d.eu = g.edge_u;

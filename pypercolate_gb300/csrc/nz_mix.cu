@@ -9,14 +9,16 @@
 // Pipeline (all on the caller's stream, no host synchronisation):
 //   1. mix_class_kernel   : class of every run (threshold tables, no libm),
 //                           histogram of classes;
-//   2. mix_offsets_kernel : classes ordered by node count N descending
+//   2. mix_offsets_kernel : classes ordered by node words S descending
 //                           (longest-first scheduling) -> segment offsets;
-//   3. mix_scatter_kernel : run ids bucketed into a queue sorted by N desc;
+//                           S = l for a chain, grid_slots(L) >= L^2 for a
+//                           grid, whose sites sit in 4 x 2 blocks per sector;
+//   3. mix_scatter_kernel : run ids bucketed into a queue sorted by S desc;
 //   4. mix_slots_kernel   : node-slot offsets of the T persistent threads;
 //   5. mix_uf_kernel      : persistent union-find.  Thread t runs queue[t]
 //      first (its node slot is sized for it), then claims further items with
-//      an atomic counter; node counts only decrease along the queue, so every
-//      later item fits the slot.  Small items (4N <= smem slot) run in shared
+//      an atomic counter; S only decreases along the queue, so every later
+//      item fits the slot.  Small items (S words <= smem slot) run in shared
 //      memory.  Each run writes its exact statistics at F evenly spaced
 //      occupation checkpoints n_j = floor(j M / (F - 1)).
 //   6. mix_reduce_kernel  : per (class, checkpoint) exact integer sums of x
@@ -58,6 +60,11 @@ __device__ __forceinline__ void class_graph(const MixDev &m, uint32_t cls, uint3
     }
 }
 
+// node words a run of class cls needs: grid_slots(L) (the tiled layout) or l
+__device__ __forceinline__ uint32_t class_slots(const MixDev &m, uint32_t cls) {
+    return cls < m.n_grid ? grid_slots(m.grid_min + cls) : m.chain_min + (cls - m.n_grid);
+}
+
 __global__ void mix_class_kernel(MixDev m, uint32_t *cls, uint32_t *counts) {
     const uint64_t key = *m.key_ptr;
     for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < m.n_runs; r += gridDim.x * blockDim.x) {
@@ -67,18 +74,18 @@ __global__ void mix_class_kernel(MixDev m, uint32_t *cls, uint32_t *counts) {
     }
 }
 
-// Position of every class in the order "node count N descending, grids
-// before chains on equal N" (grid N = L^2 and chain N = l both increase with
-// the length).  Ordering by N -- not by M -- is what makes the persistent
-// threads' node slots safe: every item after position t has at most the
-// nodes of item t.
+// Position of every class in the order "node words S descending, grids
+// before chains on equal S" (grid S = grid_slots(L) and chain S = l are
+// non-decreasing in the length).  Ordering by the words a run needs -- not
+// by M -- is what makes the persistent threads' node slots safe: every item
+// after position t needs at most the words of item t.
 __global__ void mix_order_kernel(MixDev m, uint32_t *order) {
     const uint32_t n_classes = m.n_grid + m.n_chain;
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < n_classes; c += gridDim.x * blockDim.x) {
         uint32_t rank;
         if (c < m.n_grid) {
-            const uint64_t Nc = (uint64_t)(m.grid_min + c) * (m.grid_min + c);
-            // chains with more nodes: l >= Nc + 1
+            const uint64_t Nc = grid_slots(m.grid_min + c);
+            // chains with more words: l >= Nc + 1
             const uint64_t lo = Nc + 1u;
             const uint32_t more = lo > m.chain_max ? 0u
                                 : (uint32_t)(m.chain_max - (lo > m.chain_min ? lo : (uint64_t)m.chain_min) + 1u);
@@ -86,11 +93,12 @@ __global__ void mix_order_kernel(MixDev m, uint32_t *order) {
         } else {
             const uint32_t k = c - m.n_grid;
             const uint64_t Nk = (uint64_t)m.chain_min + k;
-            // grids with at least as many nodes: smallest L in range with L^2 >= Nk
+            // grids with at least as many words: smallest L in range with
+            // grid_slots(L) >= Nk
             uint32_t a = m.grid_min, b = m.grid_max + 1u;
             while (a < b) {
                 const uint32_t mid = (a + b) >> 1;
-                if ((uint64_t)mid * mid >= Nk) b = mid; else a = mid + 1u;
+                if ((uint64_t)grid_slots(mid) >= Nk) b = mid; else a = mid + 1u;
             }
             rank = (m.n_chain - 1u - k) + (m.grid_max + 1u - a);
         }
@@ -136,7 +144,7 @@ __global__ void mix_scatter_kernel(int32_t n_runs, const uint32_t *cls, uint32_t
 }
 
 // Node-slot offsets (in words) of the T persistent threads: exclusive scan of
-// N(queue[t]) for t < T (single block).
+// the words of queue[t]'s class for t < T (single block).
 __global__ void mix_slots_kernel(MixDev m, const uint32_t *queue, const uint32_t *cls, int32_t T,
                                  uint64_t *slot_off) {
     __shared__ uint64_t s[1024];
@@ -146,11 +154,7 @@ __global__ void mix_slots_kernel(MixDev m, const uint32_t *queue, const uint32_t
     for (int32_t base = 0; base < T; base += 1024) {
         const int32_t t = base + threadIdx.x;
         uint64_t v = 0;
-        if (t < T && t < m.n_runs) {
-            uint32_t kind, L, N, M;
-            class_graph(m, cls[queue[t]], kind, L, N, M);
-            v = N;
-        }
+        if (t < T && t < m.n_runs) v = class_slots(m, cls[queue[t]]);
         s[threadIdx.x] = v;
         __syncthreads();
         for (int off = 1; off < 1024; off <<= 1) {
@@ -180,12 +184,13 @@ __device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L,
                         const MixRec &out, size_t rec_base) {
     GraphDev g;
     g.kind = KIND; g.site = 0; g.wrap = 0; g.L = L; g.N = N; g.M = M;
-    g.slots = N; g.tile_cols = 0;  // row-major node ids (decode_edge, not decode_edge_slots)
+    g.tile_cols = KIND == NZ_GRAPH_GRID2D ? (L + 3u) >> 2 : 0u;  // grids in the tiled layout
+    g.slots = KIND == NZ_GRAPH_GRID2D ? grid_slots(L) : N;
     g.two_l_m1 = KIND == NZ_GRAPH_GRID2D ? 2u * L - 1u : 1u;
     g.row_edges = KIND == NZ_GRAPH_GRID2D ? (L - 1u) * g.two_l_m1 : 0u;
     g.inv_two_l_m1 = 1.0f / (float)g.two_l_m1;
     g.eu = g.ev = nullptr; g.side = nullptr;
-    for (uint32_t i = 0; i < N; ++i) node[i] = make_root(1u, node_sides<KIND>(g, i));
+    for (uint32_t i = 0; i < N; ++i) node[node_slot<KIND>(g, i)] = make_root(1u, node_sides<KIND>(g, i));
     FeistelPerm fp;
     fp.init(key, run, M);
     uint64_t t2 = N, t3 = N, t4lo = N, t4hi = 0;
@@ -203,7 +208,7 @@ __device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L,
         if (n > 0) {
             const uint32_t e = fp.at(n - 1u);
             uint32_t u, v;
-            decode_edge<KIND>(g, e, u, v);
+            decode_edge_slots<KIND>(g, e, u, v);
             uint32_t xu = u, xv = v;
             uint32_t wu = node[xu], wv = node[xv];
             for (int hops = 0; !(is_root(wu) && is_root(wv)); ++hops) {
@@ -270,8 +275,9 @@ __global__ void __launch_bounds__(256) mix_uf_kernel(MixDev m, const uint32_t *q
         const uint32_t run = queue[pos];
         uint32_t kind, L, N, M;
         class_graph(m, cls[run], kind, L, N, M);
-        uint32_t *node = (sslot && N <= smem_words) ? sslot : gslot;
-        if (node == gslot && N > slot_words) {  // cannot happen with the N-descending queue
+        const uint32_t words = class_slots(m, cls[run]);
+        uint32_t *node = (sslot && words <= smem_words) ? sslot : gslot;
+        if (node == gslot && words > slot_words) {  // cannot happen with the words-descending queue
             atomicAdd(errors, 1u);
             pos = atomicAdd(head, 1u);
             continue;

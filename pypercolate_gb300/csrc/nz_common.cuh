@@ -143,8 +143,8 @@ struct GraphDev {
     const uint8_t *side;
 };
 
-// Bond percolation on the square grid keeps its node words in blocks of
-// 4 x 2 sites, one block per 32-byte sector (block rows of (L+3)/4 blocks),
+// The square grid (bond and site percolation) keeps its node words in blocks
+// of 4 x 2 sites, one block per 32-byte sector (block rows of (L+3)/4 blocks),
 // instead of row-major: both ends of a random bond then share a sector 5/8 of
 // the time instead of 7/16, and small clusters span fewer sectors.  Node
 // words hold these slot indices as parents; the records do not depend on the
@@ -225,7 +225,7 @@ inline GraphDev make_graph_dev(const NzGraph &g, uint32_t N, uint32_t M) {
         d.row_edges = (g.length - 1u) * d.two_l_m1;
         d.inv_two_l_m1 = 1.0f / (float)d.two_l_m1;
         d.tile_cols = (g.length + 3u) >> 2;
-        if (!d.site) d.slots = grid_slots(g.length);
+        d.slots = grid_slots(g.length);
     }
     if (d.kind == NZ_GRAPH_TORUS2D) d.slots = 4u * N;
     d.eu = g.edge_u;

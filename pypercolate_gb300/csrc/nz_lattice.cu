@@ -127,12 +127,20 @@ __device__ __forceinline__ void link(uint32_t *node, uint32_t u, uint32_t v, Tal
     if (SPAN && sides == 3u) t.st.flags |= kFlagSpan;
 }
 
+// Site kernel at most 56 registers (9 CTAs of 128 per SM), like the bond
+// union-find: beside the convolution of the previous window this measured
+// 5.84e9 against 5.47e9 site additions/s (L = 256, 100,000 runs).  The torus
+// kernel keeps its 78 registers: capped it spills and measured 18 % slower.
+#ifndef NZ_SITE_MIN_BLOCKS
+#define NZ_SITE_MIN_BLOCKS 9
+#endif
+
 template <int KIND, int PERM, bool SPAN>
-__global__ void __launch_bounds__(256) site_window_kernel(UfParams p) {
+__global__ void __launch_bounds__(128, NZ_SITE_MIN_BLOCKS) site_window_kernel(UfParams p) {
     const int32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= p.n_runs) return;
     const GraphDev &g = p.g;
-    uint32_t *node = p.nodes + (size_t)r * g.slots;  // slots == N: site lattices are not tiled
+    uint32_t *node = p.nodes + (size_t)r * g.slots;
     Tally t;
     t.load(p.state[r]);
     FeistelPerm fp;
@@ -145,21 +153,31 @@ __global__ void __launch_bounds__(256) site_window_kernel(UfParams p) {
         if (n > 0) {
             i = step_index<PERM>(fp, perm, n - 1u);
             // a caller-supplied index out of range or repeated occupies nothing
-            if (i < g.N && node[i] == kEmpty) {
+            if (KIND == NZ_GRAPH_GRID2D && i < g.N) {
+                // node words in the grid's tiled layout (grid_slot)
+                const uint32_t row = i / g.L, col = i - row * g.L;
+                auto slot = [&](uint32_t rr, uint32_t cc) {
+                    return kGridTiled ? grid_slot(g.tile_cols, rr, cc) : rr * g.L + cc;
+                };
+                const uint32_t x = slot(row, col);
+                if (node[x] == kEmpty) {
+                    const uint32_t sides = node_sides<KIND>(g, i);
+                    node[x] = make_root(1u, sides);
+                    t.add_single();
+                    if (SPAN && sides == 3u) t.st.flags |= kFlagSpan;
+                    uint32_t y;
+                    if (row > 0 && node[y = slot(row - 1u, col)] != kEmpty) link<SPAN>(node, x, y, t);
+                    if (row + 1u < g.L && node[y = slot(row + 1u, col)] != kEmpty) link<SPAN>(node, x, y, t);
+                    if (col > 0 && node[y = slot(row, col - 1u)] != kEmpty) link<SPAN>(node, x, y, t);
+                    if (col + 1u < g.L && node[y = slot(row, col + 1u)] != kEmpty) link<SPAN>(node, x, y, t);
+                }
+            } else if (KIND != NZ_GRAPH_GRID2D && i < g.N && node[i] == kEmpty) {
                 const uint32_t sides = node_sides<KIND>(g, i);
                 node[i] = make_root(1u, sides);
                 t.add_single();
                 if (SPAN && sides == 3u) t.st.flags |= kFlagSpan;
-                if (KIND == NZ_GRAPH_GRID2D) {
-                    const uint32_t row = i / g.L, col = i - row * g.L;
-                    if (row > 0 && node[i - g.L] != kEmpty) link<SPAN>(node, i, i - g.L, t);
-                    if (row + 1u < g.L && node[i + g.L] != kEmpty) link<SPAN>(node, i, i + g.L, t);
-                    if (col > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
-                    if (col + 1u < g.L && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
-                } else {
-                    if (i > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
-                    if (i + 1u < g.N && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
-                }
+                if (i > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
+                if (i + 1u < g.N && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
             }
         }
         const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
@@ -332,7 +350,8 @@ bool lattice_extension(const GraphDev &g) { return g.site || g.kind == NZ_GRAPH_
 
 void launch_init_lattice_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,
                               cudaStream_t s) {
-    const uint64_t total = (uint64_t)n_runs * g.N;
+    // every word of the runs' node arrays (the grid's layout has padding slots)
+    const uint64_t total = (uint64_t)n_runs * (g.kind == NZ_GRAPH_TORUS2D ? g.N : g.slots);
     if (g.kind == NZ_GRAPH_TORUS2D)
         init_torus_cells_kernel<<<grid_for(total), 256, 0, s>>>(total, g.site ? kEmpty : make_root(1u, 0u),
                                                                  reinterpret_cast<uint4 *>(nodes));

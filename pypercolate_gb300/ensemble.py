@@ -48,7 +48,7 @@ class Ensemble:
     ps        occupation probabilities of the canonical curves
     precision 'fp32' (FP32 products, FP64 accumulation over row chunks) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
-    window    rows per union-find launch (0: sized to ~8 GiB of records)
+    window    rows per union-find launch (0: sized to ~16 GiB of records per window)
     """
 
     def __init__(self, kind='grid', length=16, ps=None, spanning=True, precision='fp32',

@@ -398,6 +398,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
+    uf_errors = ens.errors()  # runs whose union-find state came out corrupt: 0
     nat.profile_enable(False)
     prof = nat.profile_read()
     ms = e0.elapsed_time(e1) / args.steps
@@ -531,6 +532,7 @@ def main():
         'batched_vs_plain': (value / world / plain['value']) if plain else None,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
+        'union_find_errors': uf_errors,
         'e2e': {'value': e2e_value, 'unit': unit, 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h},
     }

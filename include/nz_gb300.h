@@ -308,6 +308,14 @@ int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
  * into a CUDA graph. */
 size_t nz_ensemble_workspace_bytes(const NzGraph *graph, int32_t n_runs,
                                    int32_t P, int32_t window);
+/* Runs of the last nz_ensemble call on `workspace` (same graph, n_runs, P,
+ * window) whose union-find state came out corrupt -- a find that exceeded
+ * the depth bound, which union by size makes impossible for valid state --
+ * copied to the device word *errors on `stream`.  0 in every valid use.  No
+ * counterpart in the reference (its union-find is networkx's). */
+int nz_ensemble_errors(const NzGraph *graph, int32_t n_runs, int32_t P,
+                       int32_t window, const void *workspace,
+                       size_t workspace_bytes, uint32_t *errors, void *stream);
 int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
                 uint64_t key, uint64_t run0, const double *ps, int32_t P,
                 double cutoff, int32_t window, int32_t conv_precision,

@@ -115,6 +115,9 @@ _SIGNATURES = [
      [ctypes.POINTER(NzRecords), ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32,
       ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(NzMicroAccum), _vp]),
     ('nz_canonical_merge', ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp]),
+    ('nz_ensemble_errors', ctypes.c_int,
+     [ctypes.POINTER(NzGraph), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp,
+      _vp]),
     ('nz_micro_merge', ctypes.c_int,
      [ctypes.POINTER(NzMicroAccum), ctypes.POINTER(NzMicroAccum), ctypes.c_uint32, _vp]),
     ('nz_mt_stream_permutations', ctypes.c_int,

@@ -162,6 +162,7 @@ int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs, in
     p.run0 = run0;
     p.perms = perm_src;
     p.rec = *out;
+    p.errors = nullptr;
     {
         ProfScope prof(NZ_PROF_UNION_FIND, s);
         launch_uf_window(p, mode, spanning != 0, n_runs >= 128 ? 128 : 32, s);
@@ -528,6 +529,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         ProfScope prof(NZ_PROF_SETUP, s);
         launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
         if (conv_precision == 1) launch_weights_to_f32(L.w64, L.w32, (size_t)P * L.cap, s);
+        if (cudaMemsetAsync(L.flag, 0, 4 * sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
         launch_init_runs(g, n_runs, L.nodes, L.state, L.flag, s);
         if (cudaMemsetAsync(L.stats, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess)
             return NZ_ERR_CUDA;
@@ -549,6 +551,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     up.key = key;
     up.run0 = run0;
     up.perms = nullptr;
+    up.errors = L.flag + 1;  // zeroed in the set-up; read by nz_ensemble_errors
     ConvParams cp;
     cp.N = N;
     cp.n_runs = n_runs;
@@ -610,6 +613,23 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     // join: `s` continues after everything on s2
     if (joiner.join_now() != NZ_OK) return NZ_ERR_CUDA;
     return check_launch();
+}
+
+int nz_ensemble_errors(const NzGraph *graph, int32_t n_runs, int32_t P, int32_t window, const void *workspace,
+                       size_t workspace_bytes, uint32_t *errors, void *stream) {
+    uint32_t N, M;
+    if (!graph || !workspace || !errors || n_runs <= 0 || P <= 0) return NZ_ERR_INVALID;
+    int st = graph_size(*graph, N, M);
+    if (st) return st;
+    GraphDev g = make_graph_dev(*graph, N, M);
+    Carver c{static_cast<uint8_t *>(const_cast<void *>(workspace)), 0, workspace_bytes};
+    EnsembleLayout L;
+    ensemble_layout(c, g, n_runs, P, kDefaultCutoff, window, L);
+    if (!c.ok()) return NZ_ERR_WORKSPACE;
+    return cudaMemcpyAsync(errors, L.flag + 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, as_stream(stream)) ==
+                   cudaSuccess
+               ? NZ_OK
+               : NZ_ERR_CUDA;
 }
 
 // --------------------------------------------------------- batched uneven

@@ -20,6 +20,7 @@ struct UfParams {
     uint64_t key, run0;     // NZ_PERM_PHILOX
     const uint32_t *perms;  // [n_runs][M] otherwise
     NzRecords rec;          // row n of run r at plane[(n - n_begin) * run_stride + r]
+    uint32_t *errors;       // if set: +1 per run whose state is corrupt after its last row
 };
 
 // nz_uf.cu

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(128, NZ_SITE_MIN_BLOCKS) site_window_kernel(Uf
     }
     t.st.max = t.mx;
     p.state[r] = t.st;
+    if (p.errors && (t.st.flags & kFlagCorrupt) && p.n_end == g.M + 1u) atomicAdd(p.errors, 1u);
 }
 
 // ------------------------------------------------------ torus with wrapping
@@ -286,6 +287,7 @@ __global__ void __launch_bounds__(256) torus_window_kernel(UfParams p) {
     }
     t.st.max = t.mx;
     p.state[r] = t.st;
+    if (p.errors && (t.st.flags & kFlagCorrupt) && p.n_end == g.M + 1u) atomicAdd(p.errors, 1u);
 }
 
 // ------------------------------------------------------------ initialisers

@@ -149,6 +149,9 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
     }
     st.max = mx;
     p.state[r] = st;
+    // a find that exceeded the depth bound (only possible with corrupted
+    // state: union by size keeps trees log2 N deep) is reported once per run
+    if (p.errors && (st.flags & kFlagCorrupt) && p.n_end == g.M + 1u) atomicAdd(p.errors, 1u);
 }
 
 // ------------------------------------------------------- permutation kernels

@@ -114,7 +114,21 @@ class Ensemble:
                              micro, nat.stream_handle(stream))
         nat.check(st, 'nz_ensemble')
         self.ledger.append((int(key), int(run0), n_runs))
+        self._last_runs = n_runs
         return self
+
+    def errors(self):
+        """Runs of the last `run` whose union-find state came out corrupt (a
+        find over the depth bound): 0 in every valid use (synchronises)."""
+        if self._ws is None:
+            return 0
+        torch = nat.torch_cuda()
+        out = torch.zeros(1, dtype=torch.int32, device='cuda')
+        st = nat.lib_handle().nz_ensemble_errors(self.spec.struct(), self._last_runs, self.P,
+                                                 self.window, nat.ptr(self._ws), self._ws.numel(),
+                                                 nat.ptr(out), nat.stream_handle())
+        nat.check(st, 'nz_ensemble_errors')
+        return int(out.cpu().numpy()[0])
 
     # ------------------------------------------------------------------ state
     def state_meta(self):

@@ -84,6 +84,7 @@ def test_fused_micro_reductions_exact(gpu, oracle, window):
     L, R = 10, 97
     ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True, window=window)
     ens.run(R, key=11, run0=5)
+    assert ens.errors() == 0  # no run's union-find state came out corrupt
     got = ens.micro_sums()
     M = 2 * L * (L - 1)
     N = L * L

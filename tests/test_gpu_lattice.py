@@ -80,6 +80,7 @@ def test_ensemble_reductions_match_census(gpu, oracle, kind, model, wrap, L):
     ps = np.linspace(0.05, 0.95, 19)
     ens = Ensemble(kind, L, ps, precision='fp64', micro=True, model=model, wrap=wrap)
     ens.run(R, key=8, run0=100)
+    assert ens.errors() == 0
     q = np.zeros((R, steps + 1, 7))
     sums = np.zeros((6, steps + 1), dtype=object)
     n = np.arange(steps + 1)

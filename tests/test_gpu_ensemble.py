@@ -176,3 +176,30 @@ def test_m4_high_plane_either_side_of_its_bound(gpu, oracle, L):
         run = oracle.lattice_run(0, L, oracle.philox_permutation(21, r, M))
         m4 += run['moments_u64'][:, 4].astype(object) + run['moments_hi'][:, 4].astype(object) * (1 << 64)
     assert (got['sums'][5] == m4).all()
+
+
+def test_chain_spanning_is_exactly_p_to_the_bonds(gpu):
+    """A chain spans only once every bond is in, so each run's canonical
+    spanning value is the binomial weight of n = M: p^M, with zero spread."""
+    from pypercolate_gb300.ensemble import Ensemble
+    l = 100
+    ps = np.array([0.9, 0.97, 0.999])
+    ens = Ensemble('chain', l, ps, precision='fp64', micro=False)
+    ens.run(500, key=3, run0=0)
+    ca = ens.canonical_averages()
+    np.testing.assert_allclose(ca['percolation_probability_mean'], ps ** (l - 1), rtol=1e-12)
+    assert np.all(np.abs(ca['percolation_probability_m2']) < 1e-20)
+
+
+def test_square_grid_spans_half_the_time_at_one_half(gpu):
+    """Bond percolation on the square lattice is self-dual at p = 1/2, so the
+    top-to-bottom spanning probability of an L x L grid tends to 1/2; at
+    L = 128 over 20,000 runs it lies within 5 standard errors plus 0.02 of
+    it.  (A biased bond order -- e.g. a permutation over-representing some
+    rows early -- moves it well away.)"""
+    from pypercolate_gb300.ensemble import Ensemble
+    R = 20000
+    ens = Ensemble('grid', 128, np.array([0.5]), precision='fp64', micro=False)
+    ens.run(R, key=99, run0=0)
+    got = float(ens.canonical_averages()['percolation_probability_mean'][0])
+    assert abs(got - 0.5) < 5 * np.sqrt(0.25 / R) + 0.02, got

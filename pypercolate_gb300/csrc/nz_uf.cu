@@ -82,11 +82,18 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
 
     const NzRecords rec = p.rec;
     uint32_t mx = st.max;
+    // the permutation element of the next step is computed while this
+    // step's first node loads are in flight
+    uint32_t e_next = 0;
+    {
+        const uint32_t first = p.n_begin > 0 ? p.n_begin - 1u : 0u;
+        if (first < g.M) e_next = (PERM == NZ_PERM_PHILOX) ? fp.at(first) : __ldg(perm + first);
+    }
     for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
         uint32_t e = 0;
         if (n > 0) {
             const uint32_t idx = n - 1u;
-            e = (PERM == NZ_PERM_PHILOX) ? fp.at(idx) : __ldg(perm + idx);
+            e = e_next;
             uint32_t u, v;
             if (PERM != NZ_PERM_PHILOX && e >= g.M) {
                 u = v = 0;  // caller-supplied index out of range: no bond added
@@ -97,6 +104,8 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
             // two interleaved finds with path splitting
             uint32_t xu = u, xv = v;
             uint32_t wu = node[xu], wv = node[xv];
+            if (idx + 1u < g.M)
+                e_next = (PERM == NZ_PERM_PHILOX) ? fp.at(idx + 1u) : __ldg(perm + idx + 1u);
             // union by size keeps every tree at most log2(N) <= 21 levels deep;
             // the hop limit only guards against corrupted input state
             for (int hops = 0; !(is_root(wu) && is_root(wv)); ++hops) {

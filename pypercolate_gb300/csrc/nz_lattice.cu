@@ -148,10 +148,18 @@ __global__ void __launch_bounds__(128, NZ_SITE_MIN_BLOCKS) site_window_kernel(Uf
     if (PERM == NZ_PERM_PHILOX) fp.init(p.key, p.run0 + (uint64_t)r, g.M);
     else perm = p.perms + (size_t)r * g.M;
     const NzRecords rec = p.rec;
+    // the next step's site is computed while this step's first load is in
+    // flight (on every path, so that it always advances)
+    uint32_t i_next = 0;
+    {
+        const uint32_t first = p.n_begin > 0 ? p.n_begin - 1u : 0u;
+        if (first < g.M) i_next = step_index<PERM>(fp, perm, first);
+    }
     for (uint32_t n = p.n_begin; n < p.n_end; ++n) {
         uint32_t i = 0;
         if (n > 0) {
-            i = step_index<PERM>(fp, perm, n - 1u);
+            i = i_next;
+            bool advanced = false;
             // a caller-supplied index out of range or repeated occupies nothing
             if (KIND == NZ_GRAPH_GRID2D && i < g.N) {
                 // node words in the grid's tiled layout (grid_slot)
@@ -160,7 +168,10 @@ __global__ void __launch_bounds__(128, NZ_SITE_MIN_BLOCKS) site_window_kernel(Uf
                     return kGridTiled ? grid_slot(g.tile_cols, rr, cc) : rr * g.L + cc;
                 };
                 const uint32_t x = slot(row, col);
-                if (node[x] == kEmpty) {
+                const uint32_t wx = node[x];
+                if (n < g.M) i_next = step_index<PERM>(fp, perm, n);
+                advanced = true;
+                if (wx == kEmpty) {
                     const uint32_t sides = node_sides<KIND>(g, i);
                     node[x] = make_root(1u, sides);
                     t.add_single();
@@ -179,6 +190,7 @@ __global__ void __launch_bounds__(128, NZ_SITE_MIN_BLOCKS) site_window_kernel(Uf
                 if (i > 0 && node[i - 1u] != kEmpty) link<SPAN>(node, i, i - 1u, t);
                 if (i + 1u < g.N && node[i + 1u] != kEmpty) link<SPAN>(node, i, i + 1u, t);
             }
+            if (!advanced && n < g.M) i_next = step_index<PERM>(fp, perm, n);
         }
         const size_t off = (size_t)(n - p.n_begin) * rec.run_stride + r;
         t.write(rec, off, SPAN && (t.st.flags & kFlagSpan), i);

@@ -640,9 +640,6 @@ __device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
     return t;
 }
 
-// One block per row n: reduces all statistics of that row over the runs and
-// merges them into the accumulators (pairwise formula for M2).
-template <int BLOCK>
 // 3 resident blocks of 256 threads per SM (at most 80 registers, a few
 // hundred bytes of spills): beside the union-find of the next window this
 // measured 1364 against 1394 ms per 100,000-run L = 256 step at 100
@@ -651,6 +648,10 @@ template <int BLOCK>
 #define NZ_MICRO_MIN_BLOCKS 3
 #endif
 #define NZ_MICRO_BOUNDS __launch_bounds__(BLOCK, NZ_MICRO_MIN_BLOCKS)
+
+// One block per row n: reduces all statistics of that row over the runs and
+// merges them into the accumulators (pairwise formula for M2).
+template <int BLOCK>
 __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const uint32_t n = p.n_begin + blockIdx.x;
     const size_t row = (size_t)(n - p.n_begin) * p.rec.run_stride;

@@ -298,8 +298,10 @@ int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
  * permutation -> union-find -> (optional) fused microcanonical reductions
  * -> banded canonical convolution at P probabilities -> pairwise merge.
  * Results are merged into (acc_count, acc_mean[P*7], acc_m2[P*7]) and, if
- * micro != NULL, into *micro.  conv_precision: 0 = FP64, 1 = FP32 with
- * FP64 chunk accumulation.  The union-find runs on `stream`; the reductions
+ * micro != NULL, into *micro.  conv_precision: 0 = FP64 over each band
+ * of `cutoff` (log B >= log B(mode) - cutoff); 1 = FP32 products with FP64
+ * chunk accumulation over the rows of the band whose weights are >= e^-30 x
+ * the mode's (the weights left out sum to < 1e-13).  The union-find runs on `stream`; the reductions
  * and the convolution of each window of records run on a second stream of
  * the library's (one per concurrent call and device, created on first use
  * and kept), overlapping the union-find of the next window, and are joined

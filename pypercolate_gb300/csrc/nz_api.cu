@@ -374,6 +374,7 @@ struct EnsembleLayout {
     uint32_t *flag;
     NzRecords rec[2];  // double-buffered record windows
     uint32_t *band_lo, *band_len;
+    uint32_t *band_lo32, *band_len32;  // the FP32 convolution's bands
     double *w64;
     float *w32;
     double *stats;
@@ -384,6 +385,9 @@ struct EnsembleLayout {
 };
 
 constexpr double kDefaultCutoff = 80.0;
+// the FP32 convolution uses the rows whose weights are >= e^-30 x the mode's
+// (the rest sum to < 1e-13)
+constexpr double kConvF32Cutoff = 30.0;
 constexpr uint64_t kM4HighFreeNodes = 115001;  // max_s s^3 (N - s) < 2^64 for N <= 115,000
 
 // A second stream per device on which nz_ensemble runs the consumers of each
@@ -485,6 +489,8 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     L.band_len = c.take<uint32_t>(P);
     L.w64 = c.take<double>((size_t)P * L.cap);
     L.w32 = c.take<float>((size_t)P * L.cap);
+    L.band_lo32 = c.take<uint32_t>(P);
+    L.band_len32 = c.take<uint32_t>(P);
     L.stats = c.take<double>((size_t)n_runs * P * 7);
     L.slices = n_runs < 1024 ? 1 : (n_runs < 65536 ? 16 : 64);
     L.part = c.take<double>((size_t)L.slices * P * 7 * 3);
@@ -528,7 +534,9 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     {
         ProfScope prof(NZ_PROF_SETUP, s);
         launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
-        if (conv_precision == 1) launch_weights_to_f32(L.w64, L.w32, (size_t)P * L.cap, s);
+        if (conv_precision == 1)
+            launch_narrow_weights_f32(L.w64, L.band_lo, L.band_len, P, L.cap, exp(-fmin(cutoff, kConvF32Cutoff)),
+                                      L.w32, L.band_lo32, L.band_len32, s);
         if (cudaMemsetAsync(L.flag, 0, 4 * sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
         launch_init_runs(g, n_runs, L.nodes, L.state, L.flag, s);
         if (cudaMemsetAsync(L.stats, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess)
@@ -558,8 +566,8 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.spanning = spanning;
     cp.P = P;
     cp.cap = L.cap;
-    cp.band_lo = L.band_lo;
-    cp.band_len = L.band_len;
+    cp.band_lo = conv_precision == 1 ? L.band_lo32 : L.band_lo;
+    cp.band_len = conv_precision == 1 ? L.band_len32 : L.band_len;
     cp.w64 = L.w64;
     cp.w32 = L.w32;
     cp.acc = L.stats;

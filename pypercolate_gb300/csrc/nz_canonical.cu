@@ -475,16 +475,52 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
     }
 }
 
-__global__ void f64_to_f32_kernel(const double *a, float *b, size_t n) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        b[i] = (float)a[i];
+// Weights of the FP32 convolution: the part of each p's band whose weights
+// are at least `rel` times the band's largest, converted to FP32 and re-based
+// at its own low edge (w32[i * cap + j] is the weight of row lo32[i] + j).
+// The band of the FP64 path reaches weights e^-80 below its mode; at rel =
+// e^-30 (7.7 standard deviations from the mode) the weights left out sum to
+// less than 1e-13, far below the FP32 rounding of the sums, and the rows each
+// p reads shrink by 40 %.  Band weights are unimodal, so the kept part is one
+// run of rows.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double *w64, const uint32_t *band_lo,
+                                                                   const uint32_t *band_len, int32_t cap, double rel,
+                                                                   float *w32, uint32_t *lo32, uint32_t *len32) {
+    __shared__ double s_max[BLOCK / 32];
+    __shared__ uint32_t s_a[BLOCK / 32], s_b[BLOCK / 32];
+    const int pi = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double *w = w64 + (size_t)pi * cap;
+    const uint32_t len = min(band_len[pi], (uint32_t)cap);
+    double m = 0.0;
+    for (uint32_t j = threadIdx.x; j < len; j += BLOCK) m = fmax(m, w[j]);
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) s_max[warp] = m;
+    __syncthreads();
+    m = s_max[0];
+    for (int k = 1; k < BLOCK / 32; ++k) m = fmax(m, s_max[k]);
+    const double thr = m * rel;
+    uint32_t a = 0xffffffffu, b = 0;
+    for (uint32_t j = threadIdx.x; j < len; j += BLOCK)
+        if (w[j] >= thr) { a = min(a, j); b = max(b, j + 1); }
+    for (int o = 16; o > 0; o >>= 1) {
+        a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+    }
+    if (lane == 0) { s_a[warp] = a; s_b[warp] = b; }
+    __syncthreads();
+    a = s_a[0]; b = s_b[0];
+    for (int k = 1; k < BLOCK / 32; ++k) { a = min(a, s_a[k]); b = max(b, s_b[k]); }
+    if (b <= a) a = b = 0;  // an empty band stays empty
+    if (threadIdx.x == 0) { lo32[pi] = band_lo[pi] + a; len32[pi] = b - a; }
+    float *o = w32 + (size_t)pi * cap;
+    for (uint32_t j = threadIdx.x; j < (uint32_t)cap; j += BLOCK) o[j] = j < b - a ? (float)w[a + j] : 0.0f;
 }
 
-void launch_weights_to_f32(const double *w64, float *w32, size_t count, cudaStream_t s) {
-    if (!count) return;
-    size_t blocks = (count + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
-    f64_to_f32_kernel<<<(unsigned)blocks, 256, 0, s>>>(w64, w32, count);
+void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
+                               int32_t cap, double rel, float *w32, uint32_t *lo32, uint32_t *len32, cudaStream_t s) {
+    if (P <= 0) return;
+    narrow_weights_f32_kernel<256><<<P, 256, 0, s>>>(w64, band_lo, band_len, cap, rel, w32, lo32, len32);
 }
 
 // =====================================================================

@@ -57,14 +57,17 @@ struct ConvParams {
     int32_t n_runs;
     int32_t spanning;
     int32_t P, cap;
-    const uint32_t *band_lo, *band_len;
+    const uint32_t *band_lo, *band_len;  // rows of w64, or of w32 on the FP32 path
     const double *w64;       // [P][cap]
-    const float *w32;        // [P][cap] (FP32 path)
+    const float *w32;        // [P][cap] (FP32 path, its own narrower bands)
     double *acc;             // [n_runs][P][7], accumulated (+=)
 };
 bool conv_grid_fits(int32_t n_runs, int32_t P);  // grid of launch_conv_window within CUDA's limits
 void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s);
-void launch_weights_to_f32(const double *w64, float *w32, size_t count, cudaStream_t s);
+// FP32 weights of the rows where each band's weight is >= rel x its largest,
+// re-based at lo32 (the convolution's FP32 band)
+void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
+                               int32_t cap, double rel, float *w32, uint32_t *lo32, uint32_t *len32, cudaStream_t s);
 // part: scratch [slices][P*7][3] doubles
 void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t *acc_count,
                         double *acc_mean, double *acc_m2, double *part, int32_t slices, cudaStream_t s);

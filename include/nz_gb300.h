@@ -301,7 +301,10 @@ int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
  * micro != NULL, into *micro.  conv_precision: 0 = FP64 over each band
  * of `cutoff` (log B >= log B(mode) - cutoff); 1 = FP32 products with FP64
  * chunk accumulation over the rows of the band whose weights are >= e^-30 x
- * the mode's (the weights left out sum to < 1e-13).  The union-find runs on `stream`; the reductions
+ * the mode's (the weights left out sum to < 1e-13); 2 = the same rows on
+ * the tensor cores (tcgen05 kind::tf32, three split products per term,
+ * FP32 chunk sums added into TwoSum pairs).  A convolution wait that gives
+ * up is counted with nz_ensemble_errors.  The union-find runs on `stream`; the reductions
  * and the convolution of each window of records run on a second stream of
  * the library's (one per concurrent call and device, created on first use
  * and kept), overlapping the union-find of the next window, and are joined

@@ -13,8 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 OUT_DIR = os.path.join(HERE, '_lib')
 LIB = os.path.join(OUT_DIR, 'libnzgb300.so')
-SOURCES = ['nz_uf.cu', 'nz_lattice.cu', 'nz_canonical.cu', 'nz_api.cu', 'nz_noalloc.cu', 'nz_mix.cu',
-           'nz_mlp.cu']
+SOURCES = ['nz_uf.cu', 'nz_lattice.cu', 'nz_canonical.cu', 'nz_conv_tc.cu', 'nz_api.cu', 'nz_noalloc.cu',
+           'nz_mix.cu', 'nz_mlp.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-Xcompiler', '-Wall',
          '-Xcompiler', '-Wno-unknown-pragmas',

@@ -278,6 +278,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
     p.w64 = weights;
     p.w32 = nullptr;
     p.acc = out;
+    p.errors = nullptr;
     launch_conv_window(p, 0, s);
     return check_launch();
 }
@@ -516,12 +517,12 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
     if (!(cutoff > 0)) cutoff = kDefaultCutoff;
     if (cutoff > kDefaultCutoff) return NZ_ERR_INVALID;  // workspace is sized for the default band
-    if (conv_precision != 0 && conv_precision != 1) return NZ_ERR_INVALID;
+    if (conv_precision < 0 || conv_precision > 2) return NZ_ERR_INVALID;
     uint32_t N, M;
     int st = graph_size(*graph, N, M);
     if (st) return st;
     if (graph->kind == NZ_GRAPH_EDGES) return NZ_ERR_INVALID;  // lattices only on the fast path
-    if (!conv_grid_fits(n_runs, P)) return NZ_ERR_TOO_LARGE;
+    if (!conv_grid_fits(n_runs, P) || !conv_tc_grid_fits(n_runs, P)) return NZ_ERR_TOO_LARGE;
     if (micro && (!micro->count || !micro->span_count || !micro->sum_lo || !micro->sum_hi || !micro->m2))
         return NZ_ERR_INVALID;
     GraphDev g = make_graph_dev(*graph, N, M);
@@ -534,7 +535,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     {
         ProfScope prof(NZ_PROF_SETUP, s);
         launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
-        if (conv_precision == 1)
+        if (conv_precision != 0)
             launch_narrow_weights_f32(L.w64, L.band_lo, L.band_len, P, L.cap, exp(-fmin(cutoff, kConvF32Cutoff)),
                                       L.w32, L.band_lo32, L.band_len32, s);
         if (cudaMemsetAsync(L.flag, 0, 4 * sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
@@ -566,11 +567,12 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.spanning = spanning;
     cp.P = P;
     cp.cap = L.cap;
-    cp.band_lo = conv_precision == 1 ? L.band_lo32 : L.band_lo;
-    cp.band_len = conv_precision == 1 ? L.band_len32 : L.band_len;
+    cp.band_lo = conv_precision != 0 ? L.band_lo32 : L.band_lo;
+    cp.band_len = conv_precision != 0 ? L.band_len32 : L.band_len;
     cp.w64 = L.w64;
     cp.w32 = L.w32;
     cp.acc = L.stats;
+    cp.errors = L.flag + 1;  // with the union-find's corruption count
     MicroParams mp;
     if (micro) {
         mp.N = N;
@@ -609,7 +611,11 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
             ProfScope prof(NZ_PROF_CONV, s2);
             cp.rec = L.rec[b];
             cp.n_begin = w0; cp.n_end = w1;
-            launch_conv_window(cp, conv_precision, s2);
+            if (conv_precision == 2) {
+                if (launch_conv_window_tc(cp, s2) != 0) return NZ_ERR_CUDA;
+            } else {
+                launch_conv_window(cp, conv_precision, s2);
+            }
         }
         if (cudaEventRecord(aux.a->consumed[b], s2) != cudaSuccess) return NZ_ERR_CUDA;
     }

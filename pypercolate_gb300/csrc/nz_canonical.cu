@@ -13,6 +13,7 @@
 #include "nz_common.cuh"
 #include "nz_internal.cuh"
 #include "nz_math.cuh"
+#include "nz_records.cuh"
 
 namespace nz {
 
@@ -223,38 +224,6 @@ void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, co
 // =====================================================================
 // Banded convolution of record windows (ensemble path)
 // =====================================================================
-// Statistic S of the record at `off` (S = 0 spanning, 1 max, 2 m0, 3 m1,
-// 4 m2, 5 m3, 6 m4; 7 = m4 of records without the m4_hi plane, whose high
-// word is zero).  The FP32 loader splits 64-bit words into 32-bit halves so
-// that every conversion stays on the FP32 pipe.
-template <int S>
-__device__ __forceinline__ double record_value(const NzRecords &rec, size_t off, uint32_t N) {
-    if (S == 0) return (rec.max_span[off] & kSpanBit) ? 1.0 : 0.0;
-    if (S == 1) return (double)(rec.max_span[off] & ~kSpanBit);
-    if (S == 2) return (double)rec.m0[off];
-    if (S == 3) return (double)(N - (rec.max_span[off] & ~kSpanBit));
-    if (S == 4) return (double)rec.m2[off];
-    if (S == 5) return (double)rec.m3[off];
-    if (S == 7) return (double)rec.m4_lo[off];
-    return fma((double)rec.m4_hi[off], 18446744073709551616.0, (double)rec.m4_lo[off]);
-}
-
-__device__ __forceinline__ float u64_to_f32(uint64_t x) {
-    return fmaf((float)(uint32_t)(x >> 32), 4294967296.0f, (float)(uint32_t)x);
-}
-
-template <int S>
-__device__ __forceinline__ float record_value_f(const NzRecords &rec, size_t off, uint32_t N) {
-    if (S == 0) return (rec.max_span[off] & kSpanBit) ? 1.0f : 0.0f;
-    if (S == 1) return (float)(rec.max_span[off] & ~kSpanBit);
-    if (S == 2) return (float)rec.m0[off];
-    if (S == 3) return (float)(N - (rec.max_span[off] & ~kSpanBit));
-    if (S == 4) return u64_to_f32(rec.m2[off]);
-    if (S == 5) return u64_to_f32(rec.m3[off]);
-    if (S == 7) return u64_to_f32(rec.m4_lo[off]);
-    return fmaf((float)rec.m4_hi[off], 18446744073709551616.0f, u64_to_f32(rec.m4_lo[off]));
-}
-
 #ifndef NZ_CONV_PT
 #define NZ_CONV_PT 8
 #endif
@@ -595,8 +564,13 @@ void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t
 //   max, m0, m1 (< 2^21) and m2 (< 2^42): d = x - x0 as int64, d^2 summed
 //     exactly (u64 / u128), and M2 = (R * sum d^2 - (sum d)^2) / R from the
 //     exact 128-bit numerator;
-//   m3, m4: d exact as a 128-bit integer, squared and summed in FP64 (the
-//     shift keeps the FP64 sum free of cancellation).
+//   m3, m4: d exact as a 128-bit integer; |d| 2^-e as two FP32 parts (its
+//     top 48 bits, 2^-47 relative), squared with an exact FP32 product and
+//     summed as an FP32 (sum, compensation) pair per thread, then in FP64
+//     across threads (the shift keeps the sum free of cancellation; the
+//     power-of-two scale 2^-e, e from N, keeps squares and sums inside FP32's
+//     range).  FP64 runs at 1/64 of the FP32 rate on this chip, and the FP64
+//     squares were most of this kernel's time.
 typedef unsigned __int128 u128;
 typedef __int128 i128;
 
@@ -641,8 +615,6 @@ __device__ __forceinline__ double i128_to_f64(i128 x) {
     return x < 0 ? -u128_to_f64((u128)(-x)) : u128_to_f64((u128)x);
 }
 
-constexpr double kTwo32 = 4294967296.0;
-
 // Per-thread partial sums of one row: for every statistic the exact sum of
 // x, the exact sum of d = x - x0 and the sum of d^2 (exact integers for
 // max, m0, m2; FP64 for m3, m4), plus the spanning count.
@@ -653,15 +625,41 @@ struct MicroPart {
     i128 sd_m3, sd_m4;
     uint64_t sq_max, sq_m0;
     u128 sq_m2;
-    double fq_m3, fq_m4;
+    float fs_m3, fc_m3, fs_m4, fc_m4;  // scaled sum of d^2 and its compensation
     uint32_t span;
 };
 
-__device__ __forceinline__ double i128_to_f64_fast(i128 d) {
-    // |d| < 2^95: hi part exact in FP64, one rounding in the final FMA
-    const int64_t hi = (int64_t)(d >> 32);
-    const uint32_t lo = (uint32_t)(uint64_t)d;
-    return fma((double)hi, kTwo32, (double)lo);
+__device__ __forceinline__ float exp2i(int k) { return __int_as_float((127 + k) << 23); }  // -126 <= k <= 127
+
+// x (< 2^96, as 64-bit halves) times 2^-e as yh + yl: yh = x's top 24
+// significant bits, yl = the next 24 (both exact in FP32; the bits below are
+// truncated: 2^-47 relative), so yh^2 carries the square and yl only small
+// corrections.
+__device__ __forceinline__ void scaled_split(uint64_t lo, uint64_t hi, int e, float &yh, float &yl) {
+    const int nb = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);
+    const int s2 = nb > 48 ? nb - 48 : 0;  // y = x >> s2 keeps min(nb, 48) bits
+    uint64_t y;
+    if (s2 == 0) y = lo;
+    else if (s2 < 64) y = (lo >> s2) | (hi << (64 - s2));
+    else y = hi >> (s2 - 64);
+    const int sh = nb > 24 ? nb - s2 - 24 : 0;  // y's top 24 bits sit above bit sh
+    const uint64_t top = y >> sh;
+    const int k = s2 - e;
+    yh = (float)(uint32_t)top * exp2i(sh + k);
+    yl = (float)(uint32_t)(y - (top << sh)) * exp2i(k);
+}
+
+// (s, c) += (yh + yl)^2: the exact product yh^2 (TwoProd by FMA), TwoSum of
+// the running sum, the cross and low terms into the compensation.
+__device__ __forceinline__ void add_square(float &s, float &c, float yh, float yl) {
+    const float p = __fmul_rn(yh, yh);
+    const float pe = fmaf(yh, yh, -p);
+    const float cross = fmaf(2.0f * yh, yl, __fmul_rn(yl, yl));
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(err, __fadd_rn(pe, cross)));
 }
 
 template <int BLOCK>
@@ -700,6 +698,11 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const uint64_t x0_m2 = rec.m2[row], x0_m3 = rec.m3[row];
     const bool has_hi = rec.m4_hi != nullptr;  // without the plane the high words are zero
     const u128 x0_m4 = ((u128)(has_hi ? rec.m4_hi[row] : 0u) << 64) | rec.m4_lo[row];
+    // scales: m3 < N^3 and m4 < N^4 (< 2^96); |d| 2^-e <= 2^40, so squares
+    // stay below 2^80 and sums below 2^111, and |d| >= 1 keeps its square
+    // above 2^-88 (FP32 normal)
+    const int nbits = 32 - __clz((int)p.N);
+    const int e3 = max(0, 3 * nbits - 40), e4 = max(0, min(4 * nbits, 96) - 40);
     MicroPart a = {};
     for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
         const size_t off = row + r;
@@ -728,10 +731,12 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
         a.sq_m0 += (uint64_t)(dm0 * dm0);
         const uint64_t ad2 = (uint64_t)(dm2 < 0 ? -dm2 : dm2);
         a.sq_m2 += (u128)ad2 * ad2;
-        const double f3 = (double)dm3;
-        a.fq_m3 = fma(f3, f3, a.fq_m3);
-        const double f4 = i128_to_f64_fast(dm4);
-        a.fq_m4 = fma(f4, f4, a.fq_m4);
+        float yh, yl;
+        scaled_split((uint64_t)(dm3 < 0 ? -dm3 : dm3), 0, e3, yh, yl);
+        add_square(a.fs_m3, a.fc_m3, yh, yl);
+        const u128 ad4 = (u128)(dm4 < 0 ? -dm4 : dm4);
+        scaled_split((uint64_t)ad4, (uint64_t)(ad4 >> 64), e4, yh, yl);
+        add_square(a.fs_m4, a.fc_m4, yh, yl);
     }
     // block sums (results valid in thread 0)
     const uint64_t span = bsum_u64<BLOCK>(a.span, s_w);
@@ -748,8 +753,8 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const u128 sq_max = block_sum_u128<BLOCK>(a.sq_max, s_u);
     const u128 sq_m0 = block_sum_u128<BLOCK>(a.sq_m0, s_u);
     const u128 sq_m2 = block_sum_u128<BLOCK>(a.sq_m2, s_u);
-    const double fq_m3 = block_sum_f64<BLOCK>(a.fq_m3, s_f);
-    const double fq_m4 = block_sum_f64<BLOCK>(a.fq_m4, s_f);
+    const double fq_m3 = ldexp(block_sum_f64<BLOCK>((double)a.fs_m3 + (double)a.fc_m3, s_f), 2 * e3);
+    const double fq_m4 = ldexp(block_sum_f64<BLOCK>((double)a.fs_m4 + (double)a.fc_m4, s_f), 2 * e4);
     if (threadIdx.x != 0) return;
     const double R = (double)p.n_runs;
     const uint64_t Rn = (uint64_t)p.n_runs;

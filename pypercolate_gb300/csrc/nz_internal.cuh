@@ -61,9 +61,13 @@ struct ConvParams {
     const double *w64;       // [P][cap]
     const float *w32;        // [P][cap] (FP32 path, its own narrower bands)
     double *acc;             // [n_runs][P][7], accumulated (+=)
+    uint32_t *errors;        // tensor-core path: counts CTAs whose waits gave up (or null)
 };
 bool conv_grid_fits(int32_t n_runs, int32_t P);  // grid of launch_conv_window within CUDA's limits
 void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s);
+// 3xTF32 tensor-core convolution (tcgen05) of the FP32 bands; 0 or -1 (launch error)
+bool conv_tc_grid_fits(int32_t n_runs, int32_t P);
+int launch_conv_window_tc(const ConvParams &p, cudaStream_t s);
 // FP32 weights of the rows where each band's weight is >= rel x its largest,
 // re-based at lo32 (the convolution's FP32 band)
 void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,

@@ -20,6 +20,9 @@ import numpy as np
 from . import _native as nat
 from . import hpc
 
+# convolution precisions, in the order of nz_ensemble's conv_precision codes
+PRECISIONS = ('fp64', 'fp32', 'tf32x3')
+
 _KINDS = {'grid': nat.GRAPH_GRID2D, 'chain': nat.GRAPH_CHAIN1D, 'torus': nat.GRAPH_TORUS2D}
 
 
@@ -46,7 +49,9 @@ class Ensemble:
     model     'bond' (the reference's model) or 'site' percolation; for site
               percolation M = N steps, and p is the site occupation probability
     ps        occupation probabilities of the canonical curves
-    precision 'fp32' (FP32 products, FP64 accumulation over row chunks) or 'fp64'
+    precision 'fp32' (FP32 SIMT products, FP64 accumulation over row chunks),
+              'tf32x3' (tensor cores: three split TF32 products per term, FP32
+              sums per 32-row chunk added into TwoSum pairs) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
     window    rows per union-find launch (0: sized to ~16 GiB of records per window)
     """
@@ -64,7 +69,7 @@ class Ensemble:
                                            dtype=np.float64))
         self.P = len(self.ps)
         self.spanning = bool(spanning)
-        self.precision = {'fp64': 0, 'fp32': 1}[precision]
+        self.precision = PRECISIONS.index(precision)
         self.window = int(window)
         self.cutoff = float(cutoff)
         self.d_ps = torch.from_numpy(self.ps.copy()).to('cuda')
@@ -134,7 +139,7 @@ class Ensemble:
     def state_meta(self):
         return {'kind': self.kind, 'model': self.model, 'wrap': self.wrap,
                 'length': self.length, 'N': self.N, 'M': self.M,
-                'spanning': self.spanning, 'precision': {0: 'fp64', 1: 'fp32'}[self.precision],
+                'spanning': self.spanning, 'precision': PRECISIONS[self.precision],
                 'window': self.window, 'cutoff': self.cutoff, 'micro': self.micro is not None}
 
     def state(self):

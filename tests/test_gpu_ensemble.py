@@ -39,13 +39,15 @@ def test_ensemble_fp64_matches_oracle(gpu, oracle, kind, L):
     np.testing.assert_allclose(ca['moments_m2'], m2[:, 2:], rtol=1e-7, atol=1e-6)
 
 
-def test_ensemble_fp32_error_budget(gpu, oracle):
-    """FP32 convolution: spanning probability and percolation strength within
-    1e-6 absolute of the FP64 pipeline; moments within 2e-6 relative."""
+@pytest.mark.parametrize('precision', ['fp32', 'tf32x3'])
+def test_ensemble_fp32_error_budget(gpu, oracle, precision):
+    """FP32 convolution (SIMT, or 3xTF32 on the tensor cores): spanning
+    probability and percolation strength within 1e-6 absolute of the FP64
+    oracle pipeline; moments within 2e-6 relative."""
     from pypercolate_gb300.ensemble import Ensemble
     ps = np.linspace(0.0, 1.0, 101)
     L, R = 32, 256
-    ens = Ensemble('grid', L, ps, precision='fp32', micro=False)
+    ens = Ensemble('grid', L, ps, precision=precision, micro=False)
     ens.run(R, key=3, run0=0)
     ca = ens.canonical_averages()
     mean, _ = _oracle_canonical(oracle, 0, L, 3, 0, R, ps)
@@ -76,12 +78,12 @@ def test_ensemble_accumulates_across_calls(gpu):
     np.testing.assert_allclose(sa['m2'], sb['m2'], rtol=1e-9, atol=1e-6)
 
 
-@pytest.mark.parametrize('window', [0, 37])
-def test_fused_micro_reductions_exact(gpu, oracle, window):
+@pytest.mark.parametrize('L,R,window', [(10, 97, 0), (10, 97, 37), (128, 9, 0)])
+def test_fused_micro_reductions_exact(gpu, oracle, L, R, window):
     """Exact per-n sums over runs of max and every moment (Python ints), the
-    spanning counts, and FP64 M2, against the oracle's exact integers."""
+    spanning counts, and M2 within 1e-9, against the oracle's exact integers
+    (L = 128: the m3 and m4 squares run scaled by 2^-5 and 2^-20)."""
     from pypercolate_gb300.ensemble import Ensemble
-    L, R = 10, 97
     ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True, window=window)
     ens.run(R, key=11, run0=5)
     assert ens.errors() == 0  # no run's union-find state came out corrupt
@@ -158,6 +160,42 @@ def test_finalized_ensemble(gpu):
     np.testing.assert_allclose(fin['percolation_strength_ci'][:, 0], lo, rtol=1e-10)
     np.testing.assert_allclose(fin['percolation_strength_ci'][:, 1], hi, rtol=1e-10)
     assert np.all(fin['p'] == ps)
+
+
+@pytest.mark.parametrize('kind,L,model,wrap,R,window', [
+    ('grid', 32, 'bond', 'either', 300, 0),
+    ('grid', 32, 'bond', 'either', 300, 97),     # 21 windows, ragged last one
+    ('grid', 340, 'bond', 'either', 3, 0),       # m4 with its high-word plane
+    ('grid', 20, 'site', 'either', 257, 0),
+    ('torus', 24, 'bond', 'both', 129, 0),
+    ('torus', 16, 'site', 'x', 130, 0),
+    ('chain', 3000, 'bond', 'either', 200, 0),
+    ('chain', 1, 'bond', 'either', 5, 0),        # M = 0: one row
+])
+def test_tensor_core_convolution_matches_fp64(gpu, kind, L, model, wrap, R, window):
+    """The tcgen05 3xTF32 convolution against the FP64 convolution of the
+    same records (same Philox runs): spanning and max / N within 1e-6
+    absolute, moments within 2e-6 relative; run counts that are not a
+    multiple of the 128-run tile, 41 probabilities (a ragged 32-p tile), and
+    windows that cut the bands."""
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.0, 1.0, 41)
+    got = {}
+    for prec in ('fp64', 'tf32x3'):
+        ens = Ensemble(kind, L, ps, precision=prec, micro=False, model=model, wrap=wrap, window=window)
+        ens.run(R, key=5, run0=11)
+        assert ens.errors() == 0
+        ca = ens.canonical_averages()
+        assert np.all(ca['number_of_runs'] == R)
+        got[prec] = (ca['percolation_probability_mean'], ca['max_cluster_size_mean'], ca['moments_mean'])
+    N = ens.N
+    (s64, x64, m64), (s32, x32, m32) = got['fp64'], got['tf32x3']
+    assert np.max(np.abs(s32 - s64)) < 1e-6
+    assert np.max(np.abs(x32 - x64)) / N < 1e-6
+    big = np.abs(m64) > 1e-12
+    assert np.all(np.abs(m32 - m64)[~big] < 1e-12)
+    if big.any():
+        assert np.max(np.abs(m32 - m64)[big] / np.abs(m64[big])) < 2e-6
 
 
 @pytest.mark.parametrize('L', [339, 340])

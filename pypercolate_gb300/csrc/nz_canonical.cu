@@ -681,6 +681,9 @@ __device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
 #ifndef NZ_MICRO_MIN_BLOCKS
 #define NZ_MICRO_MIN_BLOCKS 3
 #endif
+#ifndef NZ_MICRO_PAIR
+#define NZ_MICRO_PAIR 1
+#endif
 #define NZ_MICRO_BOUNDS __launch_bounds__(BLOCK, NZ_MICRO_MIN_BLOCKS)
 
 // One block per row n: reduces all statistics of that row over the runs and
@@ -704,23 +707,28 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     const int nbits = 32 - __clz((int)p.N);
     const int e3 = max(0, 3 * nbits - 40), e4 = max(0, min(4 * nbits, 96) - 40);
     MicroPart a = {};
-    for (int r = threadIdx.x; r < p.n_runs; r += BLOCK) {
+    struct Rec {
+        uint32_t ms, m0, m4_hi;
+        uint64_t m2, m3, m4_lo;
+    };
+    auto load = [&](int r) -> Rec {
         const size_t off = row + r;
-        const uint32_t ms = rec.max_span[off];
-        const uint32_t mx = ms & ~kSpanBit;
-        const uint32_t m0 = rec.m0[off];
-        const uint64_t m2 = rec.m2[off], m3 = rec.m3[off];
-        const u128 m4 = ((u128)(has_hi ? rec.m4_hi[off] : 0u) << 64) | rec.m4_lo[off];
-        a.span += ms >> 31;
+        return Rec{rec.max_span[off], rec.m0[off], has_hi ? rec.m4_hi[off] : 0u,
+                   rec.m2[off],       rec.m3[off], rec.m4_lo[off]};
+    };
+    auto add = [&](const Rec &q) {
+        const uint32_t mx = q.ms & ~kSpanBit;
+        const u128 m4 = ((u128)q.m4_hi << 64) | q.m4_lo;
+        a.span += q.ms >> 31;
         a.sx_max += mx;
-        a.sx_m0 += m0;
-        a.sx_m2 += m2;
-        a.sx_m3 += m3;
+        a.sx_m0 += q.m0;
+        a.sx_m2 += q.m2;
+        a.sx_m3 += q.m3;
         a.sx_m4 += m4;
         const int64_t dmax = (int64_t)mx - (int64_t)x0_max;
-        const int64_t dm0 = (int64_t)m0 - (int64_t)x0_m0;
-        const int64_t dm2 = (int64_t)m2 - (int64_t)x0_m2;
-        const int64_t dm3 = (int64_t)(m3 - x0_m3);  // |m3 - x0| < 2^63
+        const int64_t dm0 = (int64_t)q.m0 - (int64_t)x0_m0;
+        const int64_t dm2 = (int64_t)q.m2 - (int64_t)x0_m2;
+        const int64_t dm3 = (int64_t)(q.m3 - x0_m3);  // |m3 - x0| < 2^63
         const i128 dm4 = (i128)(m4 - x0_m4);
         a.sd_max += dmax;
         a.sd_m0 += dm0;
@@ -737,7 +745,18 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
         const u128 ad4 = (u128)(dm4 < 0 ? -dm4 : dm4);
         scaled_split((uint64_t)ad4, (uint64_t)(ad4 >> 64), e4, yh, yl);
         add_square(a.fs_m4, a.fc_m4, yh, yl);
+    };
+    // NZ_MICRO_PAIR: the records of two runs are loaded before either is
+    // added, so each thread keeps two records' loads in flight
+    int r = threadIdx.x;
+#if NZ_MICRO_PAIR
+    for (; r + BLOCK < p.n_runs; r += 2 * BLOCK) {
+        const Rec q0 = load(r), q1 = load(r + BLOCK);
+        add(q0);
+        add(q1);
     }
+#endif
+    for (; r < p.n_runs; r += BLOCK) add(load(r));
     // block sums (results valid in thread 0)
     const uint64_t span = bsum_u64<BLOCK>(a.span, s_w);
     const uint64_t sx_max = bsum_u64<BLOCK>(a.sx_max, s_w);

@@ -49,7 +49,9 @@ def parse():
     ap.add_argument('--runs', type=int, default=100000, help='runs per step per GPU')
     ap.add_argument('--L', type=int, default=L_DEFAULT)
     ap.add_argument('--P', type=int, default=P_DEFAULT)
-    ap.add_argument('--precision', default='fp32', choices=['fp32', 'fp64'])
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'tf32x3', 'fp64'],
+                    help="canonical convolution: FP32 SIMT (default), 3xTF32 on the tensor cores "
+                         "(tcgen05), or FP64")
     ap.add_argument('--no-micro', action='store_true')
     ap.add_argument('--window', type=int, default=0)
     ap.add_argument('--cpu-sample', type=int, default=256, help='runs in the CPU baseline sample')
@@ -419,7 +421,8 @@ def main():
     # second ceiling for the union-find: HBM's rate of scattered sector reads
     gather_rate = random_gather_rate()
     uf_adds_per_s = adds_per_launch / uf_avg_s
-    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1, 'conv': 2, 'reduce': 4}
+    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1,
+                       'conv': 1 if args.precision == 'tf32x3' else 2, 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
     # plain GPU path (one lattice per launch): chunks of runs whose records for

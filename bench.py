@@ -271,7 +271,7 @@ def precision_study(args):
                      if np.any(np.abs(ref[:, j]) > 0) else 0.0}
     line = {'study': 'canonical precision', 'L': L, 'runs': R, 'P': len(ps),
             'p_grid': '1000 uniform in [0,1] + 1000 uniform in [0.48,0.52]',
-            'compare': 'FP32 products/chunk sums (FP64 across 128-row chunks) vs FP64 '
+            'compare': 'FP32 products/chunk sums (TwoSum FP32 pairs across 128-row chunks) vs FP64 '
                        'convolution of the same exact per-step records',
             'normalisation': 'spanning as is; max and moments divided by N (finalised curves)',
             'errors': err, 'seconds': times}

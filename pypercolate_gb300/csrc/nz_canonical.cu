@@ -235,15 +235,38 @@ constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before 
 #endif
 constexpr int kConvBatch = NZ_CONV_BATCH;  // record loads in flight per thread
 
+// Window accumulator of one canonical value.  FP64 path: an FP64 sum.  FP32
+// path: the FP32 partial sums of the row chunks are added into an FP32 TwoSum
+// (sum, compensation) pair -- as accurate as an FP64 sum of them, without
+// the FP64 pipe, which runs at 1/64 of the FP32 rate on this chip.
+template <int PRECISION>
+struct ConvAcc {
+    double v = 0.0;
+    __device__ __forceinline__ void add(double x) { v += x; }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <>
+struct ConvAcc<1> {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float t = __fadd_rn(s, x);
+        const float bp = __fsub_rn(t, s);
+        c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp)));
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // grid: (run tiles, p tiles, 7 statistics).  Each thread accumulates the
 // kConvPT canonical values of its run for one statistic over the window's
 // rows, with the tile's weights staged in shared memory (zero outside each
 // p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
-// products summed in FP32 over kConvChunk rows, then added into FP64.
+// products summed in FP32 over kConvChunk rows, then added into a TwoSum
+// pair (ConvAcc<1>).
 template <int PRECISION, int S, bool SITE>
 __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                           const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
-                                          double *acc) {
+                                          ConvAcc<PRECISION> *acc) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     wtype part[kConvPT];
 #pragma unroll
@@ -275,7 +298,7 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
         for (int j = 0; j < kConvPT; ++j) part[j] = fma(s_w[i][j], q, part[j]);
     }
 #pragma unroll
-    for (int j = 0; j < kConvPT; ++j) acc[j] += (double)part[j];
+    for (int j = 0; j < kConvPT; ++j) acc[j].add(part[j]);
 }
 
 // Statistics 0 (spanning), 1 (max) and 3 (m1 = held - max) all come from the
@@ -285,7 +308,8 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
 template <int PRECISION, bool SITE>
 __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                               const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
-                                              double *acc0, double *acc1, double *acc3) {
+                                              ConvAcc<PRECISION> *acc0, ConvAcc<PRECISION> *acc1,
+                                              ConvAcc<PRECISION> *acc3) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     wtype p0[kConvPT], p1[kConvPT], p3[kConvPT];
 #pragma unroll
@@ -315,16 +339,17 @@ __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, 
     for (; i < cn; ++i) step(i, p.rec.max_span[base + (size_t)i * p.rec.run_stride]);
 #pragma unroll
     for (int j = 0; j < kConvPT; ++j) {
-        acc0[j] += (double)p0[j];
-        acc1[j] += (double)p1[j];
-        acc3[j] += (double)p3[j];
+        acc0[j].add(p0[j]);
+        acc1[j].add(p1[j]);
+        acc3[j].add(p3[j]);
     }
 }
 
 // Each thread accumulates the kConvPT canonical values of its run over the
 // window's rows, with the tile's weights staged in shared memory (zero
 // outside each p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1:
-// FP32 products summed in FP32 over kConvChunk rows, then added into FP64.
+// FP32 products summed in FP32 over kConvChunk rows, then added into a
+// TwoSum pair (ConvAcc<1>).
 // MAXSET: grid (run tiles, p tiles, 1), statistics 0, 1 and 3 from the
 // max_span plane in one pass; otherwise grid (run tiles, p tiles, 4),
 // statistics 2, 4, 5, 6 (one per z).
@@ -360,13 +385,7 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = s_range[0], nhi = s_range[1];
     if (nlo >= nhi) return;
-    double acc[kConvPT], acc0[MAXSET ? kConvPT : 1], acc3[MAXSET ? kConvPT : 1];
-#pragma unroll
-    for (int j = 0; j < kConvPT; ++j) acc[j] = 0.0;
-    if (MAXSET) {
-#pragma unroll
-        for (int j = 0; j < kConvPT; ++j) acc0[j] = acc3[j] = 0.0;
-    }
+    ConvAcc<PRECISION> acc[kConvPT], acc0[MAXSET ? kConvPT : 1], acc3[MAXSET ? kConvPT : 1];
     for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
         const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
         __syncthreads();
@@ -403,10 +422,10 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
             const int pi = p0 + j;
             if (pi >= p.P) continue;
             double *o = p.acc + ((size_t)r * p.P + pi) * 7;
-            o[s] += acc[j];
+            o[s] += acc[j].value();
             if (MAXSET) {
-                if (p.spanning) o[0] += acc0[j];
-                o[3] += acc3[j];
+                if (p.spanning) o[0] += acc0[j].value();
+                o[3] += acc3[j].value();
             }
         }
     }

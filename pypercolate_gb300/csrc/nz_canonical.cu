@@ -534,16 +534,22 @@ __global__ void reduce_runs_partial_kernel(const double *stats, int32_t n_runs, 
     const int sl = blockIdx.y;
     if (c >= cols) return;
     const int r0 = sl * slice, r1 = min(n_runs, r0 + slice);
-    double n = 0, mean = 0, m2 = 0;
-    for (int r = r0; r < r1; ++r) {  // Welford == merging (1, x, 0)
-        const double x = stats[(size_t)r * cols + c];
-        n += 1.0;
-        const double d = x - mean;
-        mean += d / n;
-        m2 += d * (x - mean);
+    // sums of the deviations from the slice's first value, x0: mean = x0 +
+    // S1 / n, M2 = S2 - S1^2 / n (the shift keeps the difference free of
+    // cancellation).  Welford's update needs an FP64 division per value, and
+    // FP64 runs at 1/64 of the FP32 rate on this chip.
+    double x0 = 0.0, s1 = 0.0, s2 = 0.0;
+    if (r0 < r1) x0 = stats[(size_t)r0 * cols + c];
+    for (int r = r0 + 1; r < r1; ++r) {
+        const double d = stats[(size_t)r * cols + c] - x0;
+        s1 += d;
+        s2 = fma(d, d, s2);
     }
+    const double n = (double)max(r1 - r0, 0);
     double *o = part + ((size_t)sl * cols + c) * 3;
-    o[0] = n; o[1] = mean; o[2] = m2;
+    o[0] = n;
+    o[1] = n > 0 ? x0 + s1 / n : 0.0;
+    o[2] = n > 0 ? fmax(s2 - s1 * s1 / n, 0.0) : 0.0;
 }
 
 __global__ void reduce_runs_final_kernel(const double *part, int32_t cols, int32_t slices, const uint64_t *acc_count,

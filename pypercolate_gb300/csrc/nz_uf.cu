@@ -32,14 +32,33 @@ __device__ __forceinline__ void add128(uint64_t &lo, uint64_t &hi, uint64_t blo,
 }
 
 // ------------------------------------------------------------ initialisers
+// Initial word of node slot j: every node a singleton root with its spanning
+// sides.  Slots are written in order (coalesced) and mapped back to their
+// node; padding slots of the tiled grid layout (never read) get 0.
 template <int KIND>
-__global__ void init_nodes_kernel(GraphDev g, int32_t n_runs, uint32_t *nodes) {
-    const uint64_t total = (uint64_t)n_runs * g.N;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t r = i / g.N;
-        const uint32_t k = (uint32_t)(i - r * g.N);
-        nodes[r * g.slots + node_slot<KIND>(g, k)] = make_root(1u, node_sides<KIND>(g, k));
+__device__ __forceinline__ uint32_t init_word(const GraphDev &g, uint32_t j) {
+    uint32_t k = j;
+    if (KIND == NZ_GRAPH_GRID2D && kGridTiled) {
+        const uint32_t tile = j >> 3, w = j & 7u;
+        const uint32_t tr = tile / g.tile_cols, tc = tile - tr * g.tile_cols;
+        const uint32_t r = 2u * tr + (w >> 2), c = 4u * tc + (w & 3u);
+        if (r >= g.L || c >= g.L) return 0u;
+        k = r * g.L + c;
+    }
+    if (k >= g.N) return 0u;
+    return make_root(1u, node_sides<KIND>(g, k));
+}
+
+// block b: chunk b % chunks (kInitChunk slots) of run b / chunks
+constexpr uint32_t kInitChunk = 4096;
+template <int KIND>
+__global__ void init_nodes_kernel(GraphDev g, uint64_t blocks, uint32_t chunks, uint32_t *nodes) {
+    for (uint64_t b = blockIdx.x; b < blocks; b += gridDim.x) {
+        const uint64_t r = b / chunks;
+        const uint32_t ch = (uint32_t)(b - r * chunks);
+        uint32_t *row = nodes + r * g.slots;
+        const uint32_t j1 = min(g.slots, (ch + 1u) * kInitChunk);
+        for (uint32_t j = ch * kInitChunk + threadIdx.x; j < j1; j += blockDim.x) row[j] = init_word<KIND>(g, j);
     }
 }
 
@@ -306,11 +325,11 @@ __global__ void pack_rows_kernel(NzRecords rec, int32_t run, uint32_t N, uint32_
 // ------------------------------------------------------------ launchers
 template <int KIND>
 static void launch_init_nodes_k(const GraphDev &g, int32_t n_runs, uint32_t *nodes, cudaStream_t s) {
-    uint64_t total = (uint64_t)n_runs * g.N;
-    uint64_t blocks = (total + 255) / 256;
-    if (blocks > 152ull * 64) blocks = 152ull * 64;
-    if (blocks == 0) blocks = 1;
-    init_nodes_kernel<KIND><<<(unsigned)blocks, 256, 0, s>>>(g, n_runs, nodes);
+    const uint32_t chunks = (g.slots + kInitChunk - 1) / kInitChunk;
+    const uint64_t blocks = (uint64_t)n_runs * chunks;
+    if (blocks == 0) return;
+    const uint64_t grid = blocks < 152ull * 256 ? blocks : 152ull * 256;
+    init_nodes_kernel<KIND><<<(unsigned)grid, 256, 0, s>>>(g, blocks, chunks, nodes);
 }
 
 void launch_init_runs(const GraphDev &g, int32_t n_runs, uint32_t *nodes, RunState *state,

@@ -53,7 +53,7 @@ class Ensemble:
               'tf32x3' (tensor cores: three split TF32 products per term, FP32
               sums per 32-row chunk added into TwoSum pairs) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
-    window    rows per union-find launch (0: sized to ~16 GiB of records per window)
+    window    rows per union-find launch (0: sized to ~32 GiB of records per window)
     """
 
     def __init__(self, kind='grid', length=16, ps=None, spanning=True, precision='fp32',

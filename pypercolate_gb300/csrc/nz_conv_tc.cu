@@ -5,14 +5,14 @@
 // W[p][n] of each probability's band, every CTA computes
 //   C[run][p] += sum_n Q[n][run] W[p][n]
 // for 128 runs (M, one TMEM lane each) and 32 probabilities (N) over the
-// rows its probabilities' bands share with the window (K), in chunks of 32
+// rows its probabilities' bands share with the window (K), in chunks of 16
 // rows.  The CTA's threads load the records of a chunk (thread t = run t,
 // coalesced across the warp), convert them to FP32 and split each value into
 // TF32 hi + lo parts (round to nearest: x = hi + lo to 2^-22 relative), do the
 // same for the weights, and write both into shared memory in the canonical
 // no-swizzle K-major layout; one thread then issues
 //   D  = A_hi B_hi + A_hi B_lo + A_lo B_hi
-// as 3 x 4 MMAs of 128 x 32 x 8 into an FP32 TMEM accumulator and commits
+// as 3 x 2 MMAs of 128 x 32 x 8 into an FP32 TMEM accumulator and commits
 // them to an mbarrier.  While those run, the threads stage the next chunk;
 // afterwards they read the chunk's 32 sums of their run out of TMEM and add
 // them into FP32 TwoSum pairs (value + compensation: the sums over the whole
@@ -33,15 +33,21 @@ namespace {
 
 constexpr int kTcRuns = 128;  // M: runs per CTA
 constexpr int kTcP = 32;      // N: probabilities per CTA
-constexpr int kTcK = 32;      // rows per chunk: 4 MMAs of K = 8
+// 16-row chunks: 165 registers and 41 KB of shared memory per CTA, against
+// 231-255 and 82 KB with 32 (1216 vs 1234 ms per 100,000-run L = 256 step)
+#ifndef NZ_TC_K
+#define NZ_TC_K 16
+#endif
+constexpr int kTcK = NZ_TC_K;  // rows per chunk (16 or 32): kTcK / 8 MMAs of K = 8
+static_assert(kTcK == 16 || kTcK == 32, "chunk of 16 or 32 rows");
 constexpr uint32_t kTcCols = 2 * kTcP;                // TMEM columns: two FP32 accumulators
 constexpr uint32_t kCoreBytes = 128;                  // core matrix: 8 rows x 16 bytes
-constexpr uint32_t kSbo = (kTcK / 4) * kCoreBytes;    // between 8-row groups (1024 bytes)
+constexpr uint32_t kSbo = (kTcK / 4) * kCoreBytes;    // between 8-row groups
 constexpr uint64_t kWaitNs = 1000000000ull;           // mbarrier waits give up after 1 s
 
 struct TcShared {
-    float a[2][2][kTcRuns * kTcK];  // [stage][hi, lo] records, 16 KB each
-    float b[2][2][kTcP * kTcK];     // [stage][hi, lo] weights, 4 KB each
+    float a[2][2][kTcRuns * kTcK];  // [stage][hi, lo] records
+    float b[2][2][kTcP * kTcK];     // [stage][hi, lo] weights
     uint64_t mbar[2];               // MMAs of the chunk in each stage done
     uint32_t tmem;                  // TMEM base address
     uint32_t lo[kTcP], len[kTcP];   // FP32 bands of the CTA's probabilities
@@ -212,8 +218,10 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     const size_t base = (size_t)(nlo - p.n_begin) * stride + (size_t)(live ? r : 0);
     // thread t's row of A: 8-row group t / 8, row t % 8 of each core matrix
     const int a_off = (t >> 3) * (int)(kSbo / 4) + (t & 7) * 4;
-    // weights staged by thread t: probability j = t / 4, rows 8 (t % 4) .. + 7
-    const int wj = t >> 2, wk = (t & 3) * 8;
+    // weights staged by thread t: probability j = t / 4, rows (t % 4) kTcK / 4
+    // .. + kTcK / 4 - 1
+    constexpr int kWRows = kTcK / 4;
+    const int wj = t >> 2, wk = (t & 3) * kWRows;
     const int b_off = (wj >> 3) * (int)(kSbo / 4) + (wj & 7) * 4 + (wk / 4) * 32;
     const uint32_t wlo = sh.lo[wj], wlen = sh.len[wj];
     const float *wrow = p.w32 + (size_t)(p0 + wj) * p.cap;
@@ -252,15 +260,15 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
             }
         }
         {
-            float w[8];
+            float w[kWRows];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
+            for (int q = 0; q < kWRows; ++q) {
                 const uint32_t n = c0 + wk + q;
                 w[q] = (n < nhi && n - wlo < wlen) ? wrow[n - wlo] : 0.0f;
             }
             float *bh = sh.b[st][0] + b_off, *bl = sh.b[st][1] + b_off;
 #pragma unroll
-            for (int h2 = 0; h2 < 2; ++h2) {
+            for (int h2 = 0; h2 < kWRows / 4; ++h2) {
                 float4 h, l;
                 split_tf32(w[4 * h2 + 0], h.x, l.x);
                 split_tf32(w[4 * h2 + 1], h.y, l.y);
@@ -333,13 +341,16 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     }
 }
 
-// grid (run tiles, probability tiles of 32, 7 statistics)
-template <bool SITE>
+// grid (run tiles, probability tiles of 32, statistics): HI = false: the 7
+// statistics, or 0..5 when the records carry m4 high words; HI = true: m4
+// with its high words alone (its wider loads would otherwise set the
+// register count of every statistic's code).
+template <bool SITE, bool HI>
 __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     TcShared &sh = *reinterpret_cast<TcShared *>(tc_smem);
     const int z = blockIdx.z;
-    if (z == 0 && !p.spanning) return;
+    if (!HI && z == 0 && !p.spanning) return;
     const int p0 = blockIdx.y * kTcP;
     if (threadIdx.x < kTcP) {
         const int pi = p0 + threadIdx.x;
@@ -357,6 +368,10 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = sh.range[0], nhi = sh.range[1];
     if (nlo >= nhi) return;
+    if (HI) {
+        conv_tc_tile<6, SITE>(p, sh, p0, nlo, nhi);
+        return;
+    }
     switch (z) {
         case 0: conv_tc_tile<0, SITE>(p, sh, p0, nlo, nhi); break;
         case 1: conv_tc_tile<1, SITE>(p, sh, p0, nlo, nhi); break;
@@ -364,25 +379,29 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
         case 3: conv_tc_tile<3, SITE>(p, sh, p0, nlo, nhi); break;
         case 4: conv_tc_tile<4, SITE>(p, sh, p0, nlo, nhi); break;
         case 5: conv_tc_tile<5, SITE>(p, sh, p0, nlo, nhi); break;
-        default:
-            if (p.rec.m4_hi) conv_tc_tile<6, SITE>(p, sh, p0, nlo, nhi);
-            else conv_tc_tile<7, SITE>(p, sh, p0, nlo, nhi);
-            break;
+        default: conv_tc_tile<7, SITE>(p, sh, p0, nlo, nhi); break;
     }
 }
 
-template <bool SITE>
-cudaError_t launch_tc(const ConvParams &p, cudaStream_t s) {
+template <bool SITE, bool HI>
+cudaError_t launch_tc_k(const ConvParams &p, unsigned stats, cudaStream_t s) {
     static bool configured = false;  // per process: the attribute is per function
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE, HI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)sizeof(TcShared));
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    dim3 grid((p.n_runs + kTcRuns - 1) / kTcRuns, (p.P + kTcP - 1) / kTcP, 7);
-    conv_tc_kernel<SITE><<<grid, kTcRuns, sizeof(TcShared), s>>>(p);
+    dim3 grid((p.n_runs + kTcRuns - 1) / kTcRuns, (p.P + kTcP - 1) / kTcP, stats);
+    conv_tc_kernel<SITE, HI><<<grid, kTcRuns, sizeof(TcShared), s>>>(p);
     return cudaGetLastError();
+}
+
+template <bool SITE>
+cudaError_t launch_tc(const ConvParams &p, cudaStream_t s) {
+    if (!p.rec.m4_hi) return launch_tc_k<SITE, false>(p, 7, s);
+    const cudaError_t e = launch_tc_k<SITE, false>(p, 6, s);
+    return e != cudaSuccess ? e : launch_tc_k<SITE, true>(p, 1, s);
 }
 
 }  // namespace

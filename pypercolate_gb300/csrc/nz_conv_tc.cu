@@ -385,13 +385,11 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
 
 template <bool SITE, bool HI>
 cudaError_t launch_tc_k(const ConvParams &p, unsigned stats, cudaStream_t s) {
-    static bool configured = false;  // per process: the attribute is per function
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE, HI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(TcShared));
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+    // set on every launch (one host call per window): the attribute belongs
+    // to the function in the current device's context
+    const cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE, HI>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcShared));
+    if (e != cudaSuccess) return e;
     dim3 grid((p.n_runs + kTcRuns - 1) / kTcRuns, (p.P + kTcP - 1) / kTcP, stats);
     conv_tc_kernel<SITE, HI><<<grid, kTcRuns, sizeof(TcShared), s>>>(p);
     return cudaGetLastError();

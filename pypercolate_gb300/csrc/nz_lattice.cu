@@ -130,7 +130,8 @@ __device__ __forceinline__ void link(uint32_t *node, uint32_t u, uint32_t v, Tal
 // Site kernel at most 56 registers (9 CTAs of 128 per SM), like the bond
 // union-find: beside the convolution of the previous window this measured
 // 5.84e9 against 5.47e9 site additions/s (L = 256, 100,000 runs).  The torus
-// kernel keeps its 78 registers: capped it spills and measured 18 % slower.
+// kernel is not capped (72 registers for bonds, 78 for sites; capped, the
+// 78-register bond kernel of the time spilled and measured 18 % slower).
 #ifndef NZ_SITE_MIN_BLOCKS
 #define NZ_SITE_MIN_BLOCKS 9
 #endif

@@ -78,10 +78,12 @@ __global__ void init_state_kernel(int32_t n_runs, uint32_t N, const uint32_t *in
 }
 
 // ------------------------------------------------------------ main kernel
-// 9 resident CTAs of 128 threads per SM: at most 56 registers.  In the ensemble pipeline the union-find shares the SMs with the
-// convolution of the previous window; a smaller register footprint leaves the
-// convolution more warps: 1491 ms per 100,000-run L = 256 step against 1636
-// ms at 70 registers and 1515 ms at 48.
+// 9 resident CTAs of 128 threads per SM: at most 56 registers.  In the
+// ensemble pipeline the union-find shares the SMs with the consumers of the
+// previous window; a smaller register footprint leaves them more warps: 1491
+// ms per 100,000-run L = 256 step against 1636 ms at 70 registers and 1515 ms
+// when forced to 48 (with spills).  Since the next permutation element is
+// computed during the first loads, the kernel needs 48 without spills.
 #ifndef NZ_UF_MIN_BLOCKS
 #define NZ_UF_MIN_BLOCKS 9
 #endif

@@ -184,3 +184,10 @@ def test_surrogate_features():
     assert abs(a - b) < 1e-6
     c = S.features([1.0 - 3.0 / 1024], 1024, 'chain')
     assert c[0, 3] == 1 and abs(c[0, 4] - np.arcsinh(-3.0)) < 1e-6
+
+
+def test_precision_codes():
+    """Ensemble precision names in the order of nz_ensemble's conv_precision
+    codes (0 FP64, 1 FP32 SIMT, 2 3xTF32 tensor cores)."""
+    from pypercolate_gb300.ensemble import PRECISIONS
+    assert PRECISIONS == ('fp64', 'fp32', 'tf32x3')

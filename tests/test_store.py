@@ -107,8 +107,8 @@ def test_compatible():
     assert store.compatible(a['meta'], b['meta'], a['ps'], b['ps'])
     b['meta'] = dict(b['meta'], window=4096)  # launch shape only
     assert store.compatible(a['meta'], b['meta'], a['ps'], b['ps'])
-    for k, v in (('length', 4), ('precision', 'fp64'), ('micro', False), ('cutoff', 40.0),
-                 ('model', 'site'), ('wrap', 'x')):
+    for k, v in (('length', 4), ('precision', 'fp64'), ('precision', 'tf32x3'), ('micro', False),
+                 ('cutoff', 40.0), ('model', 'site'), ('wrap', 'x')):
         c = dict(a['meta'], **{k: v})
         assert not store.compatible(a['meta'], c, a['ps'], a['ps'])
     assert not store.compatible(a['meta'], a['meta'], a['ps'], a['ps'][:-1])

@@ -36,7 +36,7 @@ UF_BYTES_PER_ADD = 4 * 32 + 36
 # ncu capture of spanning_2d_grid(256), 12,288 runs, one 1,024-row window at
 # p ~ 0.5 (profiles/window_kernels_L256_12288_runs.md); a full launch's
 # traffic is this figure times the additions it makes
-UF_TRAFFIC_PER_ADD = 187.4
+UF_TRAFFIC_PER_ADD = 183.4
 UF_READ_PER_ADD = 90.8  # of which read (the scattered finds)
 
 

@@ -1,0 +1,106 @@
+"""CPU emulation of the compensated FP32 arithmetic the kernels use in place
+of FP64 (FP64 runs at 1/64 of the FP32 rate on GB300): the scaled two-part
+squares of micro_window_kernel (csrc/nz_canonical.cu: scaled_split,
+add_square) and the TwoSum accumulators of the convolutions (ConvAcc<1>,
+csrc/nz_conv_tc.cu: two_sum_add).  numpy float32 operations are IEEE
+round-to-nearest like the device's __fadd_rn / __fmul_rn; fmaf is emulated
+exactly with rationals.  The GPU tests check the kernels themselves against
+the oracle at the scales they reach (tests/test_gpu_ensemble.py); these pin
+the method at the scale exponents and magnitudes they do not."""
+import random
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+f32 = np.float32
+
+
+def fmaf(a, b, c):
+    """a * b + c rounded once to float32 (exact rational, then nearest)."""
+    exact = Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c))
+    r = f32(float(exact))  # may double-round; pick the nearest neighbour
+    cands = (r, np.nextafter(r, f32(np.inf)), np.nextafter(r, f32(-np.inf)))
+    return min(cands, key=lambda v: abs(Fraction(float(v)) - exact))
+
+
+def scaled_split(x, e):
+    """|d| (< 2^96) times 2^-e as (yh, yl): its top 24 significant bits and
+    the next 24, both exact in FP32 (scaled_split in nz_canonical.cu)."""
+    nb = x.bit_length()
+    s2 = nb - 48 if nb > 48 else 0
+    y = x >> s2
+    sh = nb - s2 - 24 if nb > 24 else 0
+    top = y >> sh
+    k = s2 - e
+    yh, yl = f32(top * 2.0 ** (sh + k)), f32((y - (top << sh)) * 2.0 ** k)
+    assert float(yh) == top * 2.0 ** (sh + k) and float(yl) == (y - (top << sh)) * 2.0 ** k
+    return yh, yl
+
+
+def add_square(s, c, yh, yl):
+    """(s, c) += (yh + yl)^2 as add_square in nz_canonical.cu."""
+    p = f32(yh * yh)
+    pe = fmaf(yh, yh, -p)
+    cross = fmaf(f32(2) * yh, yl, f32(yl * yl))
+    t = f32(s + p)
+    bp = f32(t - s)
+    err = f32(f32(s - f32(t - bp)) + f32(p - bp))
+    return t, f32(c + f32(err + f32(pe + cross)))
+
+
+def two_sum_add(s, c, x):
+    t = f32(s + x)
+    bp = f32(t - s)
+    return t, f32(c + f32(f32(s - f32(t - bp)) + f32(x - bp)))
+
+
+def scale_exponent(N, power):
+    """e3 / e4 of micro_window_kernel: |d| 2^-e <= 2^40 for d < N^power."""
+    nbits = int(N).bit_length()
+    return max(0, min(power * nbits, 96) - 40)
+
+
+@pytest.mark.parametrize('N,power', [(100, 3), (16384, 3), (16384, 4), (65536, 4), (115600, 4),
+                                     (2 ** 21 - 1, 3), (2 ** 21 - 1, 4)])
+def test_scaled_fp32_squares(N, power):
+    """Sum of d^2 over a thread's runs to ~1e-13 relative, for deviations up
+    to the statistic's bound (m3 < N^3, m4 < N^4 and < 2^96) down to 1, with
+    the squares and sums inside FP32's normal range."""
+    rng = random.Random(N * 10 + power)
+    e = scale_exponent(N, power)
+    bound = min(N ** power, 2 ** 96)
+    for spread in (bound, bound // 1000 + 1, 1000, 1):
+        s = c = f32(0)
+        exact = 0
+        for _ in range(400):
+            d = rng.randrange(spread + 1)
+            yh, yl = scaled_split(d, e)
+            if d:
+                assert abs(float(yh)) >= 2.0 ** -126 or float(yh) == 0.0
+            s, c = add_square(s, c, yh, yl)
+            exact += d * d
+        assert np.isfinite(s) and np.isfinite(c)
+        got = (Fraction(float(s)) + Fraction(float(c))) * Fraction(2) ** (2 * e)
+        if exact == 0:
+            assert got == 0
+        else:
+            assert abs(got - exact) / exact < 1e-12, (N, power, spread)
+
+
+def test_two_sum_accumulator_matches_exact_sum():
+    """The FP32 (sum, compensation) pair of the convolutions adds hundreds
+    of FP32 chunk sums of very different sizes as accurately as FP64 does."""
+    rng = np.random.default_rng(3)
+    xs = (rng.random(500) * 10.0 ** rng.integers(-8, 8, 500)).astype(np.float32)
+    s = c = f32(0)
+    for x in xs:
+        s, c = two_sum_add(s, c, x)
+    exact = sum(Fraction(float(x)) for x in xs)
+    got = Fraction(float(s)) + Fraction(float(c))
+    assert abs(got - exact) / exact < 1e-13
+    # a plain FP32 running sum of the same values is ~1e-8 off
+    plain = f32(0)
+    for x in xs:
+        plain = f32(plain + x)
+    assert abs(Fraction(float(plain)) - exact) / exact > 1e-10

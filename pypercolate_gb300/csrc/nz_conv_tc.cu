@@ -385,11 +385,14 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
 
 template <bool SITE, bool HI>
 cudaError_t launch_tc_k(const ConvParams &p, unsigned stats, cudaStream_t s) {
-    // set on every launch (one host call per window): the attribute belongs
-    // to the function in the current device's context
-    const cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE, HI>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcShared));
-    if (e != cudaSuccess) return e;
+    // above 48 KB of dynamic shared memory (32-row chunks) the launch needs
+    // the attribute, which belongs to the function in the current device's
+    // context: set it before every such launch
+    if constexpr (sizeof(TcShared) > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(conv_tc_kernel<SITE, HI>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TcShared));
+        if (e != cudaSuccess) return e;
+    }
     dim3 grid((p.n_runs + kTcRuns - 1) / kTcRuns, (p.P + kTcP - 1) / kTcP, stats);
     conv_tc_kernel<SITE, HI><<<grid, kTcRuns, sizeof(TcShared), s>>>(p);
     return cudaGetLastError();

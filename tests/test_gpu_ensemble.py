@@ -198,22 +198,50 @@ def test_tensor_core_convolution_matches_fp64(gpu, kind, L, model, wrap, R, wind
         assert np.max(np.abs(m32 - m64)[big] / np.abs(m64[big])) < 2e-6
 
 
+@pytest.mark.parametrize('precision', ['fp32', 'tf32x3'])
+def test_convolution_without_spanning_statistic(gpu, precision):
+    """spanning=False: no spanning fields, and the max and moment curves of
+    the FP32 paths (the tcgen05 kernel skips its spanning CTAs) within the
+    error budget of the FP64 path on the same runs."""
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.0, 1.0, 37)
+    got = {}
+    for prec in ('fp64', precision):
+        ens = Ensemble('grid', 24, ps, spanning=False, precision=prec, micro=False)
+        ens.run(150, key=9, run0=3)
+        ca = ens.canonical_averages()
+        assert 'percolation_probability_mean' not in ca.dtype.names
+        got[prec] = (ca['max_cluster_size_mean'], ca['moments_mean'])
+    (x64, m64), (x32, m32) = got['fp64'], got[precision]
+    assert np.max(np.abs(x32 - x64)) / (24 * 24) < 1e-6
+    big = np.abs(m64) > 1e-12
+    assert np.max(np.abs(m32 - m64)[big] / np.abs(m64[big])) < 2e-6
+
+
 @pytest.mark.parametrize('L', [339, 340])
 def test_m4_high_plane_either_side_of_its_bound(gpu, oracle, L):
     """Up to N = 115,000 sites the ensemble leaves out the m4 high-word
     plane (sum' s^4 < 2^64 there); L = 339 (N = 114,921) runs without it,
-    L = 340 (N = 115,600) with it.  Both give the oracle's exact sums."""
+    L = 340 (N = 115,600) with it.  Both give the oracle's exact sums, and
+    the M2 of m3 and m4 -- squared as scaled FP32 pairs, scale 2^-11 and
+    2^-28 at these sizes -- within 1e-9 of the exact integer M2."""
     from pypercolate_gb300.ensemble import Ensemble
     R = 3
     ens = Ensemble('grid', L, [0.5], precision='fp64', micro=True)
     ens.run(R, key=21, run0=0)
     got = ens.micro_sums()
     M = 2 * L * (L - 1)
-    m4 = np.zeros(M + 1, dtype=object)
-    for r in range(R):
-        run = oracle.lattice_run(0, L, oracle.philox_permutation(21, r, M))
-        m4 += run['moments_u64'][:, 4].astype(object) + run['moments_hi'][:, 4].astype(object) * (1 << 64)
-    assert (got['sums'][5] == m4).all()
+    runs = [oracle.lattice_run(0, L, oracle.philox_permutation(21, r, M)) for r in range(R)]
+    exact = {k: [run['moments_u64'][:, k].astype(object) + run['moments_hi'][:, k].astype(object) * (1 << 64)
+                 for run in runs] for k in (3, 4)}
+    assert (got['sums'][5] == sum(exact[4])).all()
+    for k, stat in ((3, 4), (4, 5)):
+        xs = exact[k]
+        s1 = sum(xs)
+        s2 = sum(x * x for x in xs)
+        # R * M2 = R * sum x^2 - (sum x)^2, exact in integers
+        m2 = np.array([float(a * R - b * b) / R for a, b in zip(s2, s1)])
+        np.testing.assert_allclose(got['m2'][stat], m2, rtol=1e-9, atol=1e-6, err_msg='m%d' % k)
 
 
 def test_chain_spanning_is_exactly_p_to_the_bonds(gpu):

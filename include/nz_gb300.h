@@ -108,6 +108,10 @@ typedef struct NzRecords {
     int64_t run_stride;
     int32_t site;       /* 0: bond records (m1 = N - max); 1: site records
                            (m1 = n - max: only occupied sites count)         */
+    int32_t narrow;     /* 0 in every record set a caller passes.  nz_ensemble
+                           sets 1 in its own windows for N <= 65,536, where
+                           m0 (< 2^16) is stored as uint16 and m2 (<= N^2/4
+                           < 2^31) as uint32 behind the same pointers       */
 } NzRecords;
 
 /* ---- library -------------------------------------------------------- */

@@ -49,7 +49,8 @@ class NzGraph(ctypes.Structure):
 class NzRecords(ctypes.Structure):
     _fields_ = [('max_span', _vp), ('m0', _vp), ('m2', _vp), ('m3', _vp),
                 ('m4_lo', _vp), ('m4_hi', _vp), ('edge', _vp),
-                ('run_stride', ctypes.c_int64), ('site', ctypes.c_int32)]
+                ('run_stride', ctypes.c_int64), ('site', ctypes.c_int32),
+                ('narrow', ctypes.c_int32)]
 
 
 class NzMicroAccum(ctypes.Structure):

@@ -75,7 +75,8 @@ struct ProfScope {
     }
 };
 
-constexpr uint32_t kRecordBytes = 4 + 4 + 8 + 8 + 8 + 4;  // planes without edge
+constexpr uint32_t kRecordBytes = 4 + 4 + 8 + 8 + 8 + 4;  // planes without edge (wide layout)
+constexpr uint32_t kNarrowRecordNodes = 65536;  // narrow records (m0 uint16, m2 uint32) up to this N
 
 
 // Workspace of the microcanonical entry point.
@@ -86,6 +87,12 @@ size_t micro_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t perm_m
     *flag = c.take<uint32_t>(4);
     *perms = perm_mode == NZ_PERM_MT19937 ? c.take<uint32_t>((size_t)n_runs * (g.M ? g.M : 1)) : nullptr;
     return c.used;
+}
+
+// A caller's record layout: wide, or narrow (m0 as uint16, m2 as uint32),
+// which holds every value only up to N = 65,536 nodes.
+bool records_layout_ok(const NzRecords &rec, uint32_t N) {
+    return rec.narrow == 0 || (rec.narrow == 1 && N <= kNarrowRecordNodes);
 }
 
 }  // namespace
@@ -134,7 +141,8 @@ int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs, in
     if (perm_mode == NZ_PERM_GIVEN && M > 0 && !perms) return NZ_ERR_INVALID;
     if (perm_mode == NZ_PERM_MT19937 && (!mt_seed_words || !mt_seed_len)) return NZ_ERR_INVALID;
     if (perm_mode < 0 || perm_mode > 2) return NZ_ERR_INVALID;
-    if (!out->max_span || !out->m0 || !out->m2 || !out->m3 || !out->m4_lo || out->run_stride < n_runs)
+    if (!out->max_span || !out->m0 || !out->m2 || !out->m3 || !out->m4_lo || out->run_stride < n_runs ||
+        !records_layout_ok(*out, N))
         return NZ_ERR_INVALID;
     GraphDev g = make_graph_dev(*graph, N, M);
     Carver c{static_cast<uint8_t *>(workspace), 0, workspace_bytes};
@@ -220,7 +228,8 @@ int nz_permutations(uint32_t num_edges, int32_t n_runs, int32_t perm_mode, uint6
 
 int nz_pack_microcanonical_rows(const NzRecords *rec, int32_t run, uint32_t num_nodes, uint32_t num_edges,
                                 int32_t spanning, uint8_t *rows, void *stream) {
-    if (!rec || !rows || run < 0 || !rec->max_span || !rec->m0 || !rec->m2 || !rec->m3 || !rec->m4_lo)
+    if (!rec || !rows || run < 0 || !rec->max_span || !rec->m0 || !rec->m2 || !rec->m3 || !rec->m4_lo ||
+        !records_layout_ok(*rec, num_nodes))
         return NZ_ERR_INVALID;
     launch_pack_rows(*rec, run, num_nodes, num_edges, spanning, rows, as_stream(stream));
     return check_launch();
@@ -261,6 +270,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
                                     int32_t spanning, const uint32_t *band_lo, const uint32_t *band_len,
                                     const double *weights, int32_t cap, int32_t P, double *out, void *stream) {
     if (!rec || !band_lo || !band_len || !weights || !out || n_runs <= 0 || P <= 0) return NZ_ERR_INVALID;
+    if (!records_layout_ok(*rec, num_nodes)) return NZ_ERR_INVALID;
     if (!conv_grid_fits(n_runs, P)) return NZ_ERR_TOO_LARGE;
     cudaStream_t s = as_stream(stream);
     if (cudaMemsetAsync(out, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess) return NZ_ERR_CUDA;
@@ -317,7 +327,7 @@ int nz_microcanonical_reduce(const NzRecords *rec, uint32_t num_nodes, uint32_t 
                              uint32_t n_begin, uint32_t n_end, const NzMicroAccum *acc, void *stream) {
     if (!rec || !acc || n_runs <= 0 || n_end <= n_begin || n_end > num_edges + 1) return NZ_ERR_INVALID;
     if (!rec->max_span || !rec->m0 || !rec->m2 || !rec->m3 || !rec->m4_lo || !rec->m4_hi ||
-        rec->run_stride < n_runs)
+        rec->run_stride < n_runs || !records_layout_ok(*rec, num_nodes))
         return NZ_ERR_INVALID;
     if (!acc->count || !acc->span_count || !acc->sum_lo || !acc->sum_hi || !acc->m2) return NZ_ERR_INVALID;
     MicroParams mp;
@@ -474,9 +484,17 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     const size_t plane = (size_t)L.window * n_runs;
     for (int b = 0; b < 2; ++b) {
         NzRecords &r = L.rec[b];
+        // up to N = 65,536 nodes m0 (< 2^16) and m2 (<= N^2/4) are stored in
+        // 16 and 32 bits: 26 instead of 32 B per record
+        r.narrow = g.N <= kNarrowRecordNodes ? 1 : 0;
         r.max_span = c.take<uint32_t>(plane);
-        r.m0 = c.take<uint32_t>(plane);
-        r.m2 = c.take<uint64_t>(plane);
+        if (r.narrow) {
+            r.m0 = reinterpret_cast<uint32_t *>(c.take<uint16_t>(plane));
+            r.m2 = reinterpret_cast<uint64_t *>(c.take<uint32_t>(plane));
+        } else {
+            r.m0 = c.take<uint32_t>(plane);
+            r.m2 = c.take<uint64_t>(plane);
+        }
         r.m3 = c.take<uint64_t>(plane);
         r.m4_lo = c.take<uint64_t>(plane);
         // sum' s^4 <= s_max^3 (N - s_max) <= max_s s^3 (N - s) < 2^64 for

@@ -405,8 +405,14 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
                 conv_rows_max<PRECISION, SITE>(p, c0, cn, r, s_w, acc0, acc, acc3);
             } else {
                 switch (s) {
-                    case 2: conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc); break;
-                    case 4: conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc); break;
+                    case 2:
+                        if (p.rec.narrow) conv_rows<PRECISION, 8, SITE>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc);
+                        break;
+                    case 4:
+                        if (p.rec.narrow) conv_rows<PRECISION, 9, SITE>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc);
+                        break;
                     case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
                     default:
                         if (p.rec.m4_hi) conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc);
@@ -722,8 +728,8 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     __shared__ double s_f[BLOCK / 32];
     __shared__ uint64_t s_w[BLOCK / 32];
     const uint32_t x0_max = rec.max_span[row] & ~kSpanBit;
-    const uint32_t x0_m0 = rec.m0[row];
-    const uint64_t x0_m2 = rec.m2[row], x0_m3 = rec.m3[row];
+    const uint32_t x0_m0 = record_m0(rec, row);
+    const uint64_t x0_m2 = record_m2(rec, row), x0_m3 = rec.m3[row];
     const bool has_hi = rec.m4_hi != nullptr;  // without the plane the high words are zero
     const u128 x0_m4 = ((u128)(has_hi ? rec.m4_hi[row] : 0u) << 64) | rec.m4_lo[row];
     // scales: m3 < N^3 and m4 < N^4 (< 2^96); |d| 2^-e <= 2^40, so squares
@@ -738,8 +744,8 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
     };
     auto load = [&](int r) -> Rec {
         const size_t off = row + r;
-        return Rec{rec.max_span[off], rec.m0[off], has_hi ? rec.m4_hi[off] : 0u,
-                   rec.m2[off],       rec.m3[off], rec.m4_lo[off]};
+        return Rec{rec.max_span[off], record_m0(rec, off), has_hi ? rec.m4_hi[off] : 0u,
+                   record_m2(rec, off), rec.m3[off],     rec.m4_lo[off]};
     };
     auto add = [&](const Rec &q) {
         const uint32_t mx = q.ms & ~kSpanBit;

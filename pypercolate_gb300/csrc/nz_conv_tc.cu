@@ -152,9 +152,12 @@ __device__ __forceinline__ void two_sum_add(float &s, float &c, float x) {
 }
 
 // Raw record words of one chunk's rows: the plane statistic S reads (m4_lo
-// for S = 6, whose m4_hi words go to `hi`).
+// for S = 6, whose m4_hi words go to `hi`; S = 8 and 9: m0 and m2 of narrow
+// records, uint16 and uint32).
 template <int S>
-using raw_word = typename std::conditional<(S >= 4), uint64_t, uint32_t>::type;
+using raw_word = typename std::conditional<
+    S == 8, uint16_t,
+    typename std::conditional<(S >= 4 && S != 9), uint64_t, uint32_t>::type>::type;
 
 template <int S>
 __device__ __forceinline__ const raw_word<S> *raw_plane(const NzRecords &rec) {
@@ -162,6 +165,8 @@ __device__ __forceinline__ const raw_word<S> *raw_plane(const NzRecords &rec) {
     else if constexpr (S == 2) return rec.m0;
     else if constexpr (S == 4) return rec.m2;
     else if constexpr (S == 5) return rec.m3;
+    else if constexpr (S == 8) return reinterpret_cast<const uint16_t *>(rec.m0);
+    else if constexpr (S == 9) return reinterpret_cast<const uint32_t *>(rec.m2);
     else return rec.m4_lo;
 }
 
@@ -185,7 +190,7 @@ template <int S>
 __device__ __forceinline__ float raw_value(raw_word<S> w, uint64_t hi, uint32_t held) {
     if constexpr (S == 0) return (w & kSpanBit) ? 1.0f : 0.0f;
     else if constexpr (S == 1) return (float)(w & ~kSpanBit);
-    else if constexpr (S == 2) return (float)w;
+    else if constexpr (S == 2 || S == 8 || S == 9) return (float)w;
     else if constexpr (S == 3) return (float)(held - (w & ~kSpanBit));
     else if constexpr (S == 6) return fmaf((float)hi, 18446744073709551616.0f, u64_to_f32(w));
     else return u64_to_f32(w);
@@ -333,7 +338,7 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
         return;
     }
     if (live) {
-        constexpr int out = S == 7 ? 6 : S;
+        constexpr int out = S == 7 ? 6 : (S == 8 ? 2 : (S == 9 ? 4 : S));
         double *o = p.acc + (size_t)r * p.P * 7;
 #pragma unroll
         for (int j = 0; j < kTcP; ++j)
@@ -375,9 +380,15 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
     switch (z) {
         case 0: conv_tc_tile<0, SITE>(p, sh, p0, nlo, nhi); break;
         case 1: conv_tc_tile<1, SITE>(p, sh, p0, nlo, nhi); break;
-        case 2: conv_tc_tile<2, SITE>(p, sh, p0, nlo, nhi); break;
+        case 2:
+            if (p.rec.narrow) conv_tc_tile<8, SITE>(p, sh, p0, nlo, nhi);
+            else conv_tc_tile<2, SITE>(p, sh, p0, nlo, nhi);
+            break;
         case 3: conv_tc_tile<3, SITE>(p, sh, p0, nlo, nhi); break;
-        case 4: conv_tc_tile<4, SITE>(p, sh, p0, nlo, nhi); break;
+        case 4:
+            if (p.rec.narrow) conv_tc_tile<9, SITE>(p, sh, p0, nlo, nhi);
+            else conv_tc_tile<4, SITE>(p, sh, p0, nlo, nhi);
+            break;
         case 5: conv_tc_tile<5, SITE>(p, sh, p0, nlo, nhi); break;
         default: conv_tc_tile<7, SITE>(p, sh, p0, nlo, nhi); break;
     }

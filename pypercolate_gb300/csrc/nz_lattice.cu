@@ -28,6 +28,7 @@
 
 #include "nz_common.cuh"
 #include "nz_internal.cuh"
+#include "nz_records.cuh"
 
 namespace nz {
 
@@ -80,8 +81,7 @@ struct Tally {
     // row n of the records
     __device__ __forceinline__ void write(const NzRecords &rec, size_t off, bool flag, uint32_t e) const {
         if (rec.max_span) rec.max_span[off] = mx | (flag ? kSpanBit : 0u);
-        if (rec.m0) rec.m0[off] = st.t0 - (st.t0 ? 1u : 0u);
-        if (rec.m2) rec.m2[off] = st.t2 - mx2;
+        put_m0_m2(rec, off, st.t0 - (st.t0 ? 1u : 0u), st.t2 - mx2);
         if (rec.m3) rec.m3[off] = st.t3 - mx3;
         const uint64_t m4_lo = st.t4_lo - mx4_lo;
         const uint64_t m4_hi = st.t4_hi - mx4_hi - (st.t4_lo < mx4_lo ? 1ull : 0ull);

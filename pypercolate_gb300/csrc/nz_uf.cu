@@ -22,6 +22,7 @@
 
 #include "nz_common.cuh"
 #include "nz_internal.cuh"
+#include "nz_records.cuh"
 
 namespace nz {
 
@@ -168,8 +169,7 @@ __global__ void NZ_UF_BOUNDS uf_window_kernel(UfParams p) {
         const uint64_t mx2 = (uint64_t)mx * mx, mx3 = mx2 * mx;
         const uint64_t mx4_lo = mx3 * mx, mx4_hi = __umul64hi(mx3, (uint64_t)mx);
         if (rec.max_span) rec.max_span[off] = mx | ((SPAN && (st.flags & kFlagSpan)) ? kSpanBit : 0u);
-        if (rec.m0) rec.m0[off] = st.t0 - 1u;
-        if (rec.m2) rec.m2[off] = st.t2 - mx2;
+        put_m0_m2(rec, off, st.t0 - 1u, st.t2 - mx2);
         if (rec.m3) rec.m3[off] = st.t3 - mx3;
         const uint64_t m4_lo = st.t4_lo - mx4_lo;
         const uint64_t m4_hi = st.t4_hi - mx4_hi - (st.t4_lo < mx4_lo ? 1ull : 0ull);
@@ -316,9 +316,9 @@ __global__ void pack_rows_kernel(NzRecords rec, int32_t run, uint32_t N, uint32_
         int o = 8;
         if (spanning) { d[8] = (ms & kSpanBit) ? 1 : 0; o = 9; }
         put_bytes(d + o, mx, 4);
-        put_bytes(d + o + 4, rec.m0[off], 8);
+        put_bytes(d + o + 4, record_m0(rec, off), 8);
         put_bytes(d + o + 12, (uint64_t)((rec.site ? n : N) - mx), 8);
-        put_bytes(d + o + 20, rec.m2[off], 8);
+        put_bytes(d + o + 20, record_m2(rec, off), 8);
         put_bytes(d + o + 28, rec.m3[off], 8);
         put_bytes(d + o + 36, rec.m4_lo[off], 8);
     }

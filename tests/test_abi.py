@@ -49,12 +49,12 @@ def test_host_only_entry_points(lib):
     assert L.nz_microcanonical_workspace_bytes(g, 10, nat.PERM_PHILOX) >= 10 * 65536 * 4
     assert L.nz_ensemble_workspace_bytes(g, 100, 1001, 0) > 100 * 65536 * 4
     # the bench's ensemble: node words (26.2 GB), two record windows sized
-    # for at most ~32 GiB each (rows counted at 36 B per record; 32 B at
-    # L = 256, without the m4 high words) and the per-run canonical
-    # accumulators (5.6 GB) -- about 93 GB of HBM
+    # for at most ~32 GiB each (rows counted at 36 B per record; 26 B at
+    # L = 256: narrow m0 and m2, no m4 high words) and the per-run canonical
+    # accumulators (5.6 GB) -- about 81 GB of HBM
     ws = L.nz_ensemble_workspace_bytes(g, 100000, 1001, 0)
     records = ws - 100000 * 65536 * 4 - 100000 * 1001 * 7 * 8
-    assert 2 * 32 * 2**30 * 32 / 36 * 0.99 < records < 2 * 32 * 2**30
+    assert 2 * 32 * 2**30 * 26 / 36 * 0.99 < records < 2 * 32 * 2**30 * 26 / 36 * 1.01
     assert L.nz_binomial_band_cap(130560, 80.0) > 2 * 12 * 181
 
 

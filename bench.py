@@ -30,14 +30,20 @@ P_DEFAULT = 1001
 KEY = 1234
 # algorithmic DRAM bytes per bond addition of the union-find kernel: four
 # random 32-byte sectors (find(u), find(v), the child pointer and the root
-# word written on a union) plus the 36 bytes of per-step records it streams
-UF_BYTES_PER_ADD = 4 * 32 + 36
+# word written on a union) plus the per-step record it streams
+
+
+def uf_bytes_per_add(N):
+    """4 x 32 B plus the record the ensemble writes per step: 26 B up to
+    N = 65,536 nodes (m0 and m2 narrow), 32 B up to 115,000 (no m4 high
+    words), 36 B above."""
+    return 4 * 32 + (26 if N <= 65536 else 32 if N <= 115000 else 36)
 # measured DRAM bytes (read + write) per bond addition of uf_window_kernel:
 # ncu capture of spanning_2d_grid(256), 12,288 runs, one 1,024-row window at
 # p ~ 0.5 (profiles/window_kernels_L256_12288_runs.md); a full launch's
 # traffic is this figure times the additions it makes
-UF_TRAFFIC_PER_ADD = 183.4
-UF_READ_PER_ADD = 90.8  # of which read (the scattered finds)
+UF_TRAFFIC_PER_ADD = 177.3
+UF_READ_PER_ADD = 90.6  # of which read (the scattered finds)
 
 
 def parse():
@@ -415,7 +421,8 @@ def main():
     uf_n, uf_ms = prof['union_find']
     adds_per_launch = R * M / max(uf_n / args.steps, 1)
     uf_avg_s = uf_ms / max(uf_n, 1) * 1e-3
-    achieved = UF_BYTES_PER_ADD * adds_per_launch / uf_avg_s / 1e9
+    uf_bytes = uf_bytes_per_add(N)
+    achieved = uf_bytes * adds_per_launch / uf_avg_s / 1e9
     peak, peak_kind = peaks()
     launches = {k: v[0] for k, v in prof.items()}
     # second ceiling for the union-find: HBM's rate of scattered sector reads
@@ -520,7 +527,7 @@ def main():
                                        'addition on a 12,288-run capture, scaled to the '
                                        'launch by its additions',
                      'kernel': 'uf_window_kernel', 'peak_source': peak_kind,
-                     'bytes_per_addition': UF_BYTES_PER_ADD,
+                     'bytes_per_addition': uf_bytes,
                      'avg_launch_ms': uf_avg_s * 1e3,
                      'random_access': {
                          'gather_sectors_per_s': gather_rate,

@@ -229,9 +229,12 @@ void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, co
 #endif
 constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
 constexpr int kConvPT = NZ_CONV_PT;    // probabilities per CTA
-constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before an FP64 flush
+constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before the TwoSum add
+// 16 record loads in flight per thread: over the FP32 band (weights >= e^-30
+// of the mode) 1047 against 1052 ms per 100,000-run L = 256 step with 8
+// (over the full e^-80 band 8 had been better: 479 against 512 ms)
 #ifndef NZ_CONV_BATCH
-#define NZ_CONV_BATCH 8
+#define NZ_CONV_BATCH 16
 #endif
 constexpr int kConvBatch = NZ_CONV_BATCH;  // record loads in flight per thread
 

@@ -40,10 +40,112 @@ def uf_bytes_per_add(N):
     return 4 * 32 + (26 if N <= 65536 else 32 if N <= 115000 else 36)
 # measured DRAM bytes (read + write) per bond addition of uf_window_kernel:
 # ncu capture of spanning_2d_grid(256), 12,288 runs, one 1,024-row window at
-# p ~ 0.5 (profiles/window_kernels_L256_12288_runs.md); a full launch's
-# traffic is this figure times the additions it makes
+# p ~ 0.5; a full launch's traffic is this figure times the additions it
+# makes
 UF_TRAFFIC_PER_ADD = 177.3
 UF_READ_PER_ADD = 90.6  # of which read (the scattered finds)
+
+
+def bench_window(M, R, window):
+    """Record-window rows of an ensemble of R runs (as nz_ensemble picks
+    them: ~32 GiB of 36-byte records per window, 256 .. M + 1 rows)."""
+    if window > 0:
+        return min(window, M + 1)
+    return int(max(256, min(M + 1, 32.0 * (1 << 30) / (R * 36))))
+
+
+def curve_errors_vs_fp64(L, ps, precision, sample, run0, window):
+    """Max absolute and relative error per canonical curve (as finalised:
+    spanning as is, the rest / N) of `precision` against the FP64
+    convolution of the same runs (the timed runs run0 .. run0 + sample - 1,
+    same record windows), for the mean and the standard deviation."""
+    import torch
+    from pypercolate_gb300.ensemble import Ensemble
+    got = {}
+    for prec in (precision, 'fp64'):
+        e = Ensemble('grid', L, ps, precision=prec, micro=False, window=window)
+        e.run(sample, key=KEY, run0=run0)
+        ca = e.canonical_averages()
+        got[prec] = (np.column_stack([ca['percolation_probability_mean'], ca['max_cluster_size_mean'],
+                                      ca['moments_mean']]),
+                     np.column_stack([ca['percolation_probability_m2'], ca['max_cluster_size_m2'],
+                                      ca['moments_m2']]))
+        N = e.N
+        del e
+        torch.cuda.empty_cache()
+    (gm, g2), (rm, r2) = got[precision], got['fp64']
+    norm = np.array([1.0] + [float(N)] * 6)
+    out = {}
+    for j, name in enumerate(STAT_NAMES):
+        a, b = gm[:, j] / norm[j], rm[:, j] / norm[j]
+        sa = np.sqrt(np.maximum(g2[:, j], 0) / (sample - 1)) / norm[j]
+        sb = np.sqrt(np.maximum(r2[:, j], 0) / (sample - 1)) / norm[j]
+        nz = np.abs(b) > 1e-12 * np.max(np.abs(b))  # relative error above the far tails
+        out[name] = {'max_abs': float(np.max(np.abs(a - b))),
+                     'max_rel': float(np.max(np.abs(a - b)[nz] / np.abs(b[nz]))) if nz.any() else 0.0,
+                     'std_max_abs': float(np.max(np.abs(sa - sb))),
+                     'curve_max': float(np.max(np.abs(b)))}
+    return {'sample_runs': sample, 'precision': precision, 'window_rows': window,
+            'criterion': 'spanning, max/N, m0/N, m1/N, m2/N: max_abs < 1e-6; m3/N, m4/N: '
+                         'max_rel < 1e-6 (relative errors where the value is >= 1e-12 of the '
+                         'curve maximum)',
+            'curves': out}
+
+
+def plain_mix_leg(counts, stream, grid=(8, 512), chain=(1024, 65536), grid_step=16,
+                  chain_step=512):
+    """The uneven workload the plain way: one lattice size per launch
+    sequence (class draw, queue, union-find with the same 256 checkpoints,
+    exact reduction), back to back on one stream, each class with the runs
+    the batched ensemble gave it (`counts`, grid classes then chain
+    classes).  Timed on a stratified sample -- every grid_step-th grid
+    length and every chain_step-th chain length -- and scaled by the strata
+    sizes into whole-workload additions and time."""
+    import torch
+    from pypercolate_gb300.mix import MixEnsemble
+    n_grid = grid[1] - grid[0] + 1
+    legs = []
+    for c in range(0, n_grid, grid_step):
+        if counts[c]:
+            L = grid[0] + c
+            legs.append(('grid', grid_step, MixEnsemble(int(counts[c]), grid=(L, L), chain=chain[:1] * 2,
+                                                        chain_share=0.0, threads=int(counts[c]))))
+    for c in range(0, chain[1] - chain[0] + 1, chain_step):
+        k = int(counts[n_grid + c])
+        if k:
+            l = chain[0] + c
+            legs.append(('chain', chain_step, MixEnsemble(k, grid=grid[:1] * 2, chain=(l, l),
+                                                          chain_share=1.0, threads=k)))
+    for _, _, e in legs[:4]:  # warm-up (module load)
+        e.run(1)
+    torch.cuda.synchronize()
+    t = {'grid': 0.0, 'chain': 0.0}
+    a = {'grid': 0, 'chain': 0}
+    step = {'grid': grid_step, 'chain': chain_step}
+    for kind in ('grid', 'chain'):
+        sel = [e for k, _, e in legs if k == kind]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for e in sel:
+            e.run(3)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t[kind] = e0.elapsed_time(e1) * 1e-3
+        a[kind] = sum(e.additions for e in sel)
+    total_t = sum(step[k] * t[k] for k in t)
+    total_a = sum(step[k] * a[k] for k in a)
+    out = {'value': total_a / total_t, 'unit': 'bond additions/s',
+           'sample': 'every %dth of %d grid lengths and every %dth of %d chain lengths, each '
+                     'with its runs of the batched workload in one launch sequence; '
+                     'whole-workload estimate = sum over strata of stride x sample'
+                     % (grid_step, n_grid, chain_step, chain[1] - chain[0] + 1),
+           'launch_sequences': len(legs),
+           'sample_seconds': {k: t[k] for k in t}, 'sample_additions': a,
+           'estimated_workload_seconds': total_t}
+    del legs
+    torch.cuda.empty_cache()
+    return out
 
 
 def parse():
@@ -65,6 +167,10 @@ def parse():
     ap.add_argument('--plain-runs', type=int, default=8192,
                     help='runs timed on the plain path (0: skip)')
     ap.add_argument('--plain-chunk', type=int, default=4096)
+    ap.add_argument('--no-plain-mix', dest='plain_mix', action='store_false',
+                    help='skip the one-lattice-per-launch timing of the uneven workload')
+    ap.add_argument('--curve-sample', type=int, default=2048,
+                    help='timed runs re-run in FP64 for the per-curve error (0: skip)')
     ap.add_argument('--mix-runs', type=int, default=1000000,
                     help='runs of the batched uneven workload (0: skip)')
     ap.add_argument('--study', default=None, choices=[None, 'precision', 'surrogate'],
@@ -432,14 +538,25 @@ def main():
                        'conv': 1 if args.precision == 'tf32x3' else 2, 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
+    # per-curve error of the timed arithmetic against FP64, on a sample of
+    # the timed runs (outside the timed region)
+    curve_err = None
+    if args.curve_sample > 0 and default_leg:
+        curve_err = curve_errors_vs_fp64(L, ps, args.precision, min(args.curve_sample, R),
+                                         run_base + args.warmup * R, bench_window(M, R, args.window))
+
     # plain GPU path (one lattice per launch): chunks of runs whose records for
-    # all M+1 rows are materialised by one union-find launch, FP64 convolution
+    # all M+1 rows are materialised by one union-find launch, then reduced
+    # and convolved by separate launches; same kernels and arithmetic as the
+    # batched leg, without the window pipeline (nothing overlaps)
     plain = None
     if args.plain_runs > 0:
         chunk = min(args.plain_chunk, args.plain_runs)
-        pe = Ensemble('grid', L, ps, precision='fp64', micro=not args.no_micro, window=M + 1)
+        pe = Ensemble('grid', L, ps, precision=args.precision, micro=not args.no_micro, window=M + 1)
         pe.run(chunk, key=KEY, run0=run_base + 2 * 10 ** 8)  # warm-up
         torch.cuda.synchronize()
+        nat.profile_read()
+        nat.profile_enable(True)
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         p0.record(stream)
@@ -449,10 +566,16 @@ def main():
             done += chunk
         p1.record(stream)
         torch.cuda.synchronize()
+        nat.profile_enable(False)
+        pprof = nat.profile_read()
         pms = p0.elapsed_time(p1)
+        puf_n, puf_ms = pprof['union_find']
         plain = {'value': done * M / (pms * 1e-3), 'unit': 'bond additions/s', 'runs': done,
-                 'chunk': chunk, 'ms': pms,
-                 'path': 'records for all M+1 rows per launch, FP64 convolution'}
+                 'chunk': chunk, 'ms': pms, 'precision': args.precision,
+                 'union_find_only': done * M / (puf_ms * 1e-3),
+                 'kernel_ms': {k: v[1] for k, v in pprof.items()},
+                 'path': 'records for all M+1 rows per union-find launch, consumers after it '
+                         '(no overlap), same kernels and arithmetic as the batched leg'}
         del pe
         torch.cuda.empty_cache()
 
@@ -478,6 +601,7 @@ def main():
         torch.cuda.synchronize()
         mms = m0e.elapsed_time(m1e) / 2
         adds = me.additions
+        counts = me.count.cpu().numpy().astype(np.int64)
         mix = {'value': adds / (mms * 1e-3), 'unit': 'bond additions/s', 'runs': args.mix_runs,
                'additions_per_ensemble': adds, 'ms_per_ensemble': mms,
                'launch': {'threads': threads, 'block': block, 'smem_words': smem},
@@ -486,6 +610,9 @@ def main():
                            '50/50, 256 checkpoints, exact per-lattice reductions'}
         del me
         torch.cuda.empty_cache()
+        if args.plain_mix:
+            mix['plain'] = plain_mix_leg(counts, stream)
+            mix['batched_vs_plain'] = mix['value'] / mix['plain']['value']
 
     # end to end through the public API: inputs (p-grid) from pinned host
     # memory, results (finalized canonical averages) read back every step
@@ -540,6 +667,9 @@ def main():
         'plain_gpu': plain,
         'batched_uneven': mix,
         'batched_vs_plain': (value / world / plain['value']) if plain else None,
+        'union_find_only': {'batched': uf_adds_per_s,
+                            'plain': plain['union_find_only'] if plain else None},
+        'curve_err_vs_fp64': curve_err,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
         'union_find_errors': uf_errors,

@@ -152,9 +152,11 @@ int nz_microcanonical(const NzGraph *graph, int32_t spanning, int32_t n_runs,
  * 255 runs of spanning_2d_grid(256)) return NZ_ERR_TOO_LARGE.  No cudaMalloc,
  * cudaFree or allocating library routine is called (keep the nz_profile_*
  * instrumentation off on this path: when on, it creates CUDA event objects).
- * The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
+ * The array's device address is per CUDA context: the first call in each
+ * context (the device's primary context, a context the caller made current,
+ * or the new primary context after a cudaDeviceReset) looks it up
+ * (cudaGetSymbolAddress) with that context current and caches it under the
+ * context's unique ID; make that first call before any stream capture.
  * Every call shares the one array, which keeps the previous call's contents:
  * calls whose execution overlaps on the GPU (other streams, other host
  * threads) race and must be serialised by the caller.

@@ -287,6 +287,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
     p.band_len = band_len;
     p.w64 = weights;
     p.w32 = nullptr;
+    p.w32lo = nullptr;
     p.acc = out;
     p.errors = nullptr;
     launch_conv_window(p, 0, s);
@@ -387,7 +388,7 @@ struct EnsembleLayout {
     uint32_t *band_lo, *band_len;
     uint32_t *band_lo32, *band_len32;  // the FP32 convolution's bands
     double *w64;
-    float *w32;
+    float *w32, *w32lo;  // FP32 weights and their remainders
     double *stats;
     double *part;
     int32_t slices;
@@ -509,6 +510,7 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     L.band_len = c.take<uint32_t>(P);
     L.w64 = c.take<double>((size_t)P * L.cap);
     L.w32 = c.take<float>((size_t)P * L.cap);
+    L.w32lo = c.take<float>((size_t)P * L.cap);
     L.band_lo32 = c.take<uint32_t>(P);
     L.band_len32 = c.take<uint32_t>(P);
     L.stats = c.take<double>((size_t)n_runs * P * 7);
@@ -556,7 +558,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
         if (conv_precision != 0)
             launch_narrow_weights_f32(L.w64, L.band_lo, L.band_len, P, L.cap, exp(-fmin(cutoff, kConvF32Cutoff)),
-                                      L.w32, L.band_lo32, L.band_len32, s);
+                                      L.w32, L.w32lo, L.band_lo32, L.band_len32, s);
         if (cudaMemsetAsync(L.flag, 0, 4 * sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
         launch_init_runs(g, n_runs, L.nodes, L.state, L.flag, s);
         if (cudaMemsetAsync(L.stats, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess)
@@ -590,6 +592,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.band_len = conv_precision != 0 ? L.band_len32 : L.band_len;
     cp.w64 = L.w64;
     cp.w32 = L.w32;
+    cp.w32lo = L.w32lo;
     cp.acc = L.stats;
     cp.errors = L.flag + 1;  // with the union-find's corruption count
     MicroParams mp;

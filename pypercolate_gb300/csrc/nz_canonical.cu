@@ -355,7 +355,8 @@ __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, 
 // TwoSum pair (ConvAcc<1>).
 // MAXSET: grid (run tiles, p tiles, 1), statistics 0, 1 and 3 from the
 // max_span plane in one pass; otherwise grid (run tiles, p tiles, 4),
-// statistics 2, 4, 5, 6 (one per z).
+// statistics 2, 4, 5, 6 (one per z) -- on the FP32 path (run tiles, p
+// tiles, 3), statistics 2, 5, 6, with m2 (4) in conv_m2_comp_kernel.
 #ifdef NZ_CONV_MIN_BLOCKS
 #define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns, NZ_CONV_MIN_BLOCKS)
 #else
@@ -369,8 +370,10 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     __shared__ uint32_t s_range[2];
     const int r = blockIdx.x * kConvRuns + threadIdx.x;
     const int p0 = blockIdx.y * kConvPT;
+    // FP64: statistics 2, 4, 5, 6; FP32: 2, 5, 6 (m2 has its compensated kernel)
     constexpr int kOther[4] = {2, 4, 5, 6};
-    const int s = MAXSET ? 1 : kOther[blockIdx.z];
+    constexpr int kOther32[3] = {2, 5, 6};
+    const int s = MAXSET ? 1 : (PRECISION == 0 ? kOther[blockIdx.z] : kOther32[blockIdx.z]);
     if (threadIdx.x < kConvPT) {
         const int pi = p0 + threadIdx.x;
         s_lo[threadIdx.x] = pi < p.P ? p.band_lo[pi] : 0u;
@@ -440,6 +443,133 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     }
 }
 
+// ---------------------------------------------------------------------
+// m2 with compensated FP32 arithmetic
+// ---------------------------------------------------------------------
+// sum' s^2 / N is the susceptibility curve: up to ~2e4 at L = 1024, and its
+// canonical value must come within 1e-6 absolute of the FP64 convolution,
+// i.e. ~5e-11 relative per run.  Plain FP32 sums of 128 products carry
+// ~1e-7, and FP32 weights alone ~2e-9.  So every term is computed from exact
+// two-part operands and summed with its rounding errors kept, after Dot2 of
+// Ogita, Rump & Oishi (2005, "Accurate sum and dot product"):
+//   w = wh + wl        (wh = FP32(w64), wl = FP32(w64 - wh): ~2^-48 relative)
+//   q = qh + ql        (qh = q rounded toward zero to 24 bits, ql = q - qh,
+//                       both exact in FP32 for q < 2^48)
+//   ph = wh qh, eh = fma(wh, qh, -ph)     (TwoProduct: ph + eh = wh qh exactly)
+//   (s, e) = TwoSum(s, ph)                (s + e = old s + ph exactly)
+//   c += e + eh + wh ql + wl qh           (wl ql, ~2^-48 of the term, dropped)
+// The run's value is s + c (FP64), about 2^-44 relative; the statistic's
+// curve then inherits FP64-level accuracy from the FP64 run reduction.
+struct Dot2Acc {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float wh, float wl, float qh, float ql) {
+        const float ph = __fmul_rn(wh, qh);
+        const float eh = __fmaf_rn(wh, qh, -ph);
+        const float t = __fadd_rn(s, ph);
+        const float bp = __fsub_rn(t, s);
+        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(e, eh));
+        c = __fmaf_rn(wh, ql, c);
+        c = __fmaf_rn(wl, qh, c);
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// q (< 2^48) as qh + ql, both exact in FP32
+__device__ __forceinline__ void split_u64(uint64_t q, float &qh, float &ql) {
+    qh = __ull2float_rz(q);
+    ql = (float)(int64_t)(q - (uint64_t)qh);
+}
+__device__ __forceinline__ void split_u32(uint32_t q, float &qh, float &ql) {
+    qh = __uint2float_rz(q);
+    ql = (float)(int32_t)(q - (uint32_t)qh);
+}
+
+// grid (run tiles, p tiles): each thread the kConvPT m2 values of its run
+template <bool NARROW>
+__global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
+    __shared__ float s_wh[kConvChunk][kConvPT], s_wl[kConvChunk][kConvPT];
+    __shared__ uint32_t s_lo[kConvPT], s_len[kConvPT];
+    __shared__ uint32_t s_range[2];
+    const int r = blockIdx.x * kConvRuns + threadIdx.x;
+    const int p0 = blockIdx.y * kConvPT;
+    if (threadIdx.x < kConvPT) {
+        const int pi = p0 + threadIdx.x;
+        s_lo[threadIdx.x] = pi < p.P ? p.band_lo[pi] : 0u;
+        s_len[threadIdx.x] = pi < p.P ? p.band_len[pi] : 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t a = 0xffffffffu, b = 0;
+        for (int j = 0; j < kConvPT; ++j)
+            if (s_len[j]) { a = min(a, s_lo[j]); b = max(b, s_lo[j] + s_len[j]); }
+        s_range[0] = max(a, p.n_begin);
+        s_range[1] = min(b, p.n_end);
+    }
+    __syncthreads();
+    const uint32_t nlo = s_range[0], nhi = s_range[1];
+    if (nlo >= nhi) return;
+    Dot2Acc acc[kConvPT];
+    const uint32_t *m2n = reinterpret_cast<const uint32_t *>(p.rec.m2);
+    for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
+        const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < kConvChunk * kConvPT; i += kConvRuns) {
+            const int row = i / kConvPT, j = i % kConvPT;
+            const uint32_t n = c0 + row;
+            float vh = 0.0f, vl = 0.0f;
+            if (row < (int)cn && n >= s_lo[j] && n < s_lo[j] + s_len[j]) {
+                const size_t widx = (size_t)(p0 + j) * p.cap + (n - s_lo[j]);
+                vh = p.w32[widx];
+                vl = p.w32lo[widx];
+            }
+            s_wh[row][j] = vh;
+            s_wl[row][j] = vl;
+        }
+        __syncthreads();
+        if (r >= p.n_runs) continue;
+        const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
+        uint32_t i = 0;
+        for (; i + kConvBatch <= cn; i += kConvBatch) {
+            float qh[kConvBatch], ql[kConvBatch];
+#pragma unroll
+            for (int b = 0; b < kConvBatch; ++b) {
+                const size_t off = base + (size_t)(i + b) * p.rec.run_stride;
+                if (NARROW) split_u32(m2n[off], qh[b], ql[b]);
+                else split_u64(p.rec.m2[off], qh[b], ql[b]);
+            }
+#pragma unroll
+            for (int b = 0; b < kConvBatch; ++b)
+#pragma unroll
+                for (int j = 0; j < kConvPT; ++j) acc[j].add(s_wh[i + b][j], s_wl[i + b][j], qh[b], ql[b]);
+        }
+        for (; i < cn; ++i) {
+            const size_t off = base + (size_t)i * p.rec.run_stride;
+            float qh, ql;
+            if (NARROW) split_u32(m2n[off], qh, ql);
+            else split_u64(p.rec.m2[off], qh, ql);
+#pragma unroll
+            for (int j = 0; j < kConvPT; ++j) acc[j].add(s_wh[i][j], s_wl[i][j], qh, ql);
+        }
+    }
+    if (r < p.n_runs) {
+#pragma unroll
+        for (int j = 0; j < kConvPT; ++j) {
+            const int pi = p0 + j;
+            if (pi >= p.P) continue;
+            p.acc[((size_t)r * p.P + pi) * 7 + 4] += acc[j].value();
+        }
+    }
+}
+
+void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s) {
+    if (p.n_runs <= 0 || p.P <= 0) return;
+    dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
+    if (p.rec.narrow) conv_m2_comp_kernel<true><<<g, kConvRuns, 0, s>>>(p);
+    else conv_m2_comp_kernel<false><<<g, kConvRuns, 0, s>>>(p);
+}
+
 bool conv_grid_fits(int32_t n_runs, int32_t P) {
     // grid.y (p tiles) is limited to 65535
     return n_runs > 0 && P > 0 && (P + kConvPT - 1) / kConvPT <= 65535;
@@ -450,7 +580,7 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
     // (run tiles, p tiles, statistics); launching the p tiles of one run tile
     // back to back (for L2 reuse of its records) measured slower
     dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
-    dim3 gother(gmax.x, gmax.y, 4);
+    dim3 gother(gmax.x, gmax.y, precision == 0 ? 4 : 3);
     // the record model is a template parameter: a run-time test in the row
     // loop cost 17 % of the kernel's time
     if (p.rec.site) {
@@ -460,6 +590,7 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
         } else {
             conv_window_kernel<1, true, true><<<gmax, kConvRuns, 0, s>>>(p);
             conv_window_kernel<1, true, false><<<gother, kConvRuns, 0, s>>>(p);
+            launch_conv_m2_comp(p, s);
         }
     } else {
         if (precision == 0) {
@@ -468,6 +599,7 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
         } else {
             conv_window_kernel<1, false, true><<<gmax, kConvRuns, 0, s>>>(p);
             conv_window_kernel<1, false, false><<<gother, kConvRuns, 0, s>>>(p);
+            launch_conv_m2_comp(p, s);
         }
     }
 }
@@ -483,7 +615,8 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double *w64, const uint32_t *band_lo,
                                                                    const uint32_t *band_len, int32_t cap, double rel,
-                                                                   float *w32, uint32_t *lo32, uint32_t *len32) {
+                                                                   float *w32, float *w32lo, uint32_t *lo32,
+                                                                   uint32_t *len32) {
     __shared__ double s_max[BLOCK / 32];
     __shared__ uint32_t s_a[BLOCK / 32], s_b[BLOCK / 32];
     const int pi = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -511,13 +644,20 @@ __global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double 
     if (b <= a) a = b = 0;  // an empty band stays empty
     if (threadIdx.x == 0) { lo32[pi] = band_lo[pi] + a; len32[pi] = b - a; }
     float *o = w32 + (size_t)pi * cap;
-    for (uint32_t j = threadIdx.x; j < (uint32_t)cap; j += BLOCK) o[j] = j < b - a ? (float)w[a + j] : 0.0f;
+    float *ol = w32lo + (size_t)pi * cap;
+    for (uint32_t j = threadIdx.x; j < (uint32_t)cap; j += BLOCK) {
+        const double v = j < b - a ? w[a + j] : 0.0;
+        const float hi = (float)v;
+        o[j] = hi;
+        ol[j] = (float)(v - (double)hi);  // exact difference; its FP32 rounding is 2^-24 of 2^-24 w
+    }
 }
 
 void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
-                               int32_t cap, double rel, float *w32, uint32_t *lo32, uint32_t *len32, cudaStream_t s) {
+                               int32_t cap, double rel, float *w32, float *w32lo, uint32_t *lo32, uint32_t *len32,
+                               cudaStream_t s) {
     if (P <= 0) return;
-    narrow_weights_f32_kernel<256><<<P, 256, 0, s>>>(w64, band_lo, band_len, cap, rel, w32, lo32, len32);
+    narrow_weights_f32_kernel<256><<<P, 256, 0, s>>>(w64, band_lo, band_len, cap, rel, w32, w32lo, lo32, len32);
 }
 
 // =====================================================================

@@ -18,6 +18,8 @@
 // them into FP32 TwoSum pairs (value + compensation: the sums over the whole
 // band keep ~2^-44 relative accuracy without FP64, whose rate on this chip is
 // 1/64 of FP32).  Shared memory and TMEM accumulators are double-buffered.
+// m2 (the susceptibility, which needs ~5e-11 relative per run) is not done
+// here: the launcher adds the compensated SIMT kernel of nz_canonical.cu.
 //
 // Reference: the products and sums of bond_canonical_statistics
 // (percolate/hpc.py:443-515), sum_n B(M, n, p) Q_n per statistic.
@@ -346,15 +348,19 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     }
 }
 
-// grid (run tiles, probability tiles of 32, statistics): HI = false: the 7
-// statistics, or 0..5 when the records carry m4 high words; HI = true: m4
-// with its high words alone (its wider loads would otherwise set the
-// register count of every statistic's code).
+// grid (run tiles, probability tiles of 32, statistics): HI = false: the
+// statistics 0, 1, 2, 3, 5, 6, or 0, 1, 2, 3, 5 when the records carry m4
+// high words; HI = true: m4 with its high words alone (its wider loads would
+// otherwise set the register count of every statistic's code).  m2 (4) runs
+// on the compensated SIMT kernel.
 template <bool SITE, bool HI>
 __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     TcShared &sh = *reinterpret_cast<TcShared *>(tc_smem);
-    const int z = blockIdx.z;
+    // statistic of this z: m2 (4) runs on the compensated SIMT kernel
+    // (conv_m2_comp_kernel) instead
+    constexpr int kStat[6] = {0, 1, 2, 3, 5, 6};
+    const int z = kStat[blockIdx.z];
     if (!HI && z == 0 && !p.spanning) return;
     const int p0 = blockIdx.y * kTcP;
     if (threadIdx.x < kTcP) {
@@ -385,10 +391,6 @@ __global__ void __launch_bounds__(kTcRuns) conv_tc_kernel(ConvParams p) {
             else conv_tc_tile<2, SITE>(p, sh, p0, nlo, nhi);
             break;
         case 3: conv_tc_tile<3, SITE>(p, sh, p0, nlo, nhi); break;
-        case 4:
-            if (p.rec.narrow) conv_tc_tile<9, SITE>(p, sh, p0, nlo, nhi);
-            else conv_tc_tile<4, SITE>(p, sh, p0, nlo, nhi);
-            break;
         case 5: conv_tc_tile<5, SITE>(p, sh, p0, nlo, nhi); break;
         default: conv_tc_tile<7, SITE>(p, sh, p0, nlo, nhi); break;
     }
@@ -411,8 +413,8 @@ cudaError_t launch_tc_k(const ConvParams &p, unsigned stats, cudaStream_t s) {
 
 template <bool SITE>
 cudaError_t launch_tc(const ConvParams &p, cudaStream_t s) {
-    if (!p.rec.m4_hi) return launch_tc_k<SITE, false>(p, 7, s);
-    const cudaError_t e = launch_tc_k<SITE, false>(p, 6, s);
+    if (!p.rec.m4_hi) return launch_tc_k<SITE, false>(p, 6, s);
+    const cudaError_t e = launch_tc_k<SITE, false>(p, 5, s);
     return e != cudaSuccess ? e : launch_tc_k<SITE, true>(p, 1, s);
 }
 
@@ -425,7 +427,12 @@ bool conv_tc_grid_fits(int32_t n_runs, int32_t P) {
 int launch_conv_window_tc(const ConvParams &p, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return 0;
     const cudaError_t e = p.rec.site ? launch_tc<true>(p, s) : launch_tc<false>(p, s);
-    return e == cudaSuccess ? 0 : -1;
+    if (e != cudaSuccess) return -1;
+    // m2 needs ~5e-11 relative per run (the susceptibility curve within 1e-6
+    // absolute of FP64 at L = 1024), beyond FP32 tensor-core accumulation:
+    // it runs on the compensated SIMT kernel
+    launch_conv_m2_comp(p, s);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace nz

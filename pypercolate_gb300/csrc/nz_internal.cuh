@@ -60,6 +60,7 @@ struct ConvParams {
     const uint32_t *band_lo, *band_len;  // rows of w64, or of w32 on the FP32 path
     const double *w64;       // [P][cap]
     const float *w32;        // [P][cap] (FP32 path, its own narrower bands)
+    const float *w32lo;      // [P][cap] w64 - w32 as FP32 (the compensated m2 products)
     double *acc;             // [n_runs][P][7], accumulated (+=)
     uint32_t *errors;        // tensor-core path: counts CTAs whose waits gave up (or null)
 };
@@ -70,8 +71,12 @@ bool conv_tc_grid_fits(int32_t n_runs, int32_t P);
 int launch_conv_window_tc(const ConvParams &p, cudaStream_t s);
 // FP32 weights of the rows where each band's weight is >= rel x its largest,
 // re-based at lo32 (the convolution's FP32 band)
+// (and their FP32 remainders w64 - w32 in w32lo)
 void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
-                               int32_t cap, double rel, float *w32, uint32_t *lo32, uint32_t *len32, cudaStream_t s);
+                               int32_t cap, double rel, float *w32, float *w32lo, uint32_t *lo32, uint32_t *len32,
+                               cudaStream_t s);
+// m2 (statistic 4) of the FP32 paths with compensated products and sums
+void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s);
 // part: scratch [slices][P*7][3] doubles
 void launch_reduce_runs(const double *stats, int32_t n_runs, int32_t P, uint64_t *acc_count,
                         double *acc_mean, double *acc_m2, double *part, int32_t slices, cudaStream_t s);

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a container where the reference source tree is mounted::
+Run in a container where the reference source tree is mounted, passing
+its root directory::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference source tree>
 
 It imports andsor/pypercolate 0.4.6 read-only through ``refshim`` and records
 its outputs as small ``.npz`` files.  The GPU test box never runs this

@@ -104,3 +104,56 @@ def test_two_sum_accumulator_matches_exact_sum():
     for x in xs:
         plain = f32(plain + x)
     assert abs(Fraction(float(plain)) - exact) / exact > 1e-10
+
+
+def split_value(q):
+    """An integer q < 2^48 as (qh, ql): q rounded toward zero to 24
+    significant bits and the exact remainder (split_u64 / split_u32 in
+    nz_canonical.cu)."""
+    nb = q.bit_length()
+    sh = nb - 24 if nb > 24 else 0
+    qh = (q >> sh) << sh
+    return f32(qh), f32(q - qh)
+
+
+def dot2_add(s, c, wh, wl, qh, ql):
+    """One term of conv_m2_comp_kernel's compensated dot product (Dot2Acc)."""
+    ph = f32(wh * qh)
+    eh = fmaf(wh, qh, -ph)
+    t = f32(s + ph)
+    bp = f32(t - s)
+    e = f32(f32(s - f32(t - bp)) + f32(ph - bp))
+    c = f32(c + f32(e + eh))
+    c = fmaf(wh, ql, c)
+    c = fmaf(wl, qh, c)
+    return t, c
+
+
+@pytest.mark.parametrize('L,rows', [(256, 800), (1024, 1500)])
+def test_compensated_m2_products_reach_5e_11(L, rows):
+    """The m2 convolution of one run over a binomial band, with FP64
+    weights split into FP32 hi + lo and m2 values (up to N^2 / 4) split into
+    exact FP32 parts, comes within 5e-11 relative of the exact dot product
+    of the FP64 weights -- what the susceptibility curve needs to stay within
+    1e-6 absolute of FP64 at L = 1024 (m2 / N up to ~2e4) -- where plain FP32
+    products summed in FP32 are ~1e-7 off."""
+    rng = np.random.default_rng(L)
+    N = L * L
+    n = np.arange(rows)
+    w = np.exp(-0.5 * ((n - rows / 2) / (rows / 9)) ** 2)
+    w /= w.sum()
+    hi = rng.integers(1, N * N // 4, rows // 4 + 1)
+    q = [int(x) for x in np.repeat(hi, 4)[:rows] + rng.integers(0, 1000, rows)]
+    exact = sum(Fraction(float(wi)) * qi for wi, qi in zip(w, q))
+    s = c = f32(0)
+    plain = f32(0)
+    for wi, qi in zip(w, q):
+        wh = f32(wi)
+        wl = f32(float(wi) - float(wh))
+        qh, ql = split_value(qi)
+        assert int(qh) + int(ql) == qi
+        s, c = dot2_add(s, c, wh, wl, qh, ql)
+        plain = fmaf(wh, f32(qi), plain)
+    got = Fraction(float(s)) + Fraction(float(c))
+    assert abs(got - exact) / exact < 5e-11
+    assert abs(Fraction(float(plain)) - exact) / exact > 1e-9

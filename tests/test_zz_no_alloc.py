@@ -112,3 +112,39 @@ def test_noalloc_refuses_requests_beyond_its_array(gpu):
     st = lib.nz_microcanonical_noalloc(g, 1, 256, gpu.PERM_PHILOX, 0, 0, None, None, None, 1,
                                        rec.struct(), gpu.stream_handle())
     assert st == gpu.NZ_ERR_TOO_LARGE
+
+
+def test_noalloc_call_allocates_no_device_memory(gpu):
+    """Device memory in use, as the driver and torch's allocator see it, is
+    the same before and after a call (once the library's kernels are loaded
+    by a first call), with the per-kernel timing instrumentation off: that
+    instrumentation creates CUDA events and is not for this path."""
+    import torch
+    from pypercolate_gb300 import hpc
+    lib = gpu.lib_handle()
+    gpu.profile_enable(False)
+    spec = hpc.GraphSpec(gpu.GRAPH_GRID2D, 24)
+    n_runs = 33
+    g = spec.struct()
+    rec = gpu.Records(spec.M + 1, n_runs, with_edge=True)
+    rs = rec.struct()
+
+    def call(key):
+        st = lib.nz_microcanonical_noalloc(g, 1, n_runs, gpu.PERM_PHILOX, key, 0, None, None, None,
+                                           1, rs, gpu.stream_handle())
+        assert st == gpu.NZ_OK, st
+        torch.cuda.synchronize()
+
+    call(1)  # loads the kernels and takes the array's address in this context
+    free0, _ = torch.cuda.mem_get_info()
+    used0 = torch.cuda.memory_allocated()
+    reserved0 = torch.cuda.memory_reserved()
+    call(2)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == used0
+    assert torch.cuda.memory_reserved() == reserved0
+    # and the records are those of the workspace entry point
+    got = rec.host()
+    want = _run(gpu, spec, True, n_runs, gpu.PERM_PHILOX, key=2)
+    _assert_same(got, want)

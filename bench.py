@@ -92,7 +92,7 @@ def curve_errors_vs_fp64(L, ps, precision, sample, run0, window):
             'curves': out}
 
 
-def plain_mix_leg(counts, stream, grid=(8, 512), chain=(1024, 65536), grid_step=16,
+def plain_mix_leg(counts, stream, grid=(8, 512), chain=(1024, 65536), grid_step=32,
                   chain_step=512):
     """The uneven workload the plain way: one lattice size per launch
     sequence (class draw, queue, union-find with the same 256 checkpoints,
@@ -522,6 +522,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = R * M * world / (ms * 1e-3)
+    merged_runs = None
+    if world > 1:
+        # the one exchange of the multi-GPU path, after timing: every rank's
+        # ensemble state gathered and merged on the device (Ensemble.merge)
+        from pypercolate_gb300.distributed import merged_ensemble
+        merged_runs = int(merged_ensemble(ens).count.cpu().numpy()[0])
 
     # dominant kernel: union-find windows
     uf_n, uf_ms = prof['union_find']
@@ -672,6 +678,7 @@ def main():
         'curve_err_vs_fp64': curve_err,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
+        'merged_runs': merged_runs,
         'union_find_errors': uf_errors,
         'e2e': {'value': e2e_value, 'unit': unit, 'h2d_bytes_per_step': h2d,
                 'd2h_bytes_per_step': d2h},

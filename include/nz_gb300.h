@@ -202,6 +202,19 @@ int nz_binomial_weights(uint32_t num_edges, const double *ps, int32_t P,
 int nz_binomial_pmf(uint32_t num_edges, const double *ps, int32_t P,
                     double *out, void *stream);
 
+/* Replaces the sums of percolate/percolate.py:1171-1221 (canonical_averages:
+ * binomial pmf times every microcanonical average array, confidence bounds
+ * included): out[i * cols + c] = sum_j weights[i * cap + j] *
+ * values[(band_lo[i] + j) * cols + c] over the band of p_i (rows of the band
+ * at or beyond `rows` are skipped), FP64.  values: rows x cols, row-major
+ * (one row per n); bands and weights as nz_binomial_weights() writes them
+ * (the reference's full-length pmf is zero, in FP64, outside the band of
+ * cutoff 745). */
+int nz_band_dot(const uint32_t *band_lo, const uint32_t *band_len,
+                const double *weights, int32_t cap, int32_t P,
+                const double *values, uint32_t rows, int32_t cols,
+                double *out, void *stream);
+
 /* Replaces percolate/hpc.py:443-515 bond_canonical_statistics on rows in the
  * reference's packed layout: out[i * 7 + s] = sum_n f_i[n] * Q_s[n] for
  * n_factor_sets full-length factor vectors (factors[i * (M + 1) + n]), FP64. */
@@ -404,6 +417,11 @@ int nz_mlp_backward(const int32_t *widths, int32_t n_layers, int32_t batch,
                     const float *x, const void *params_bf16, const float *z,
                     const float *h, const float *dy, float *grads,
                     float *scratch, void *stream);
+/* The GEMMs of nz_mlp_forward / nz_mlp_backward run on the tensor cores
+ * (tcgen05, BF16 operands, FP32 accumulation); a tile whose tensor-core
+ * waits gave up (after 1 s) is written as NaN and counted.  Reads the count
+ * since the last call and resets it (synchronous). */
+int nz_mlp_take_errors(uint32_t *count);
 /* Adam step (step >= 1); also refreshes params_bf16 */
 int nz_mlp_adam(float *params, const float *grads, float *m, float *v,
                 void *params_bf16, int64_t count, float lr, float beta1,

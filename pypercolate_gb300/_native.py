@@ -97,6 +97,9 @@ _SIGNATURES = [
       _vp, _vp]),
     ('nz_binomial_pmf', ctypes.c_int,
      [ctypes.c_uint32, _vp, ctypes.c_int32, _vp, _vp]),
+    ('nz_band_dot', ctypes.c_int,
+     [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_uint32, ctypes.c_int32, _vp,
+      _vp]),
     ('nz_canonical_statistics_rows', ctypes.c_int,
      [_vp, ctypes.c_uint32, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp]),
     ('nz_canonical_statistics_records', ctypes.c_int,
@@ -138,6 +141,7 @@ _SIGNATURES = [
      [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp]),
     ('nz_mlp_backward', ctypes.c_int,
      [_vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ('nz_mlp_take_errors', ctypes.c_int, [_vp]),
     ('nz_mlp_adam', ctypes.c_int,
      [_vp, _vp, _vp, _vp, _vp, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
       ctypes.c_float, ctypes.c_int32, _vp]),

@@ -259,6 +259,15 @@ int nz_binomial_pmf(uint32_t num_edges, const double *ps, int32_t P, double *out
     return check_launch();
 }
 
+int nz_band_dot(const uint32_t *band_lo, const uint32_t *band_len, const double *weights, int32_t cap, int32_t P,
+                const double *values, uint32_t rows, int32_t cols, double *out, void *stream) {
+    if (!band_lo || !band_len || !weights || !values || !out || cap <= 0 || P <= 0 || cols <= 0 || rows == 0)
+        return NZ_ERR_INVALID;
+    if ((cols + 31) / 32 > 65535) return NZ_ERR_TOO_LARGE;
+    launch_band_dot(band_lo, band_len, weights, cap, P, values, rows, cols, out, as_stream(stream));
+    return check_launch();
+}
+
 int nz_canonical_statistics_rows(const uint8_t *rows, uint32_t num_edges, int32_t spanning, const double *factors,
                                  int32_t n_factor_sets, double *out, void *stream) {
     if (!rows || !factors || !out || n_factor_sets <= 0) return NZ_ERR_INVALID;
@@ -288,6 +297,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
     p.w64 = weights;
     p.w32 = nullptr;
     p.w32lo = nullptr;
+    p.core_lo = p.core_len = nullptr;
     p.acc = out;
     p.errors = nullptr;
     launch_conv_window(p, 0, s);
@@ -387,6 +397,7 @@ struct EnsembleLayout {
     NzRecords rec[2];  // double-buffered record windows
     uint32_t *band_lo, *band_len;
     uint32_t *band_lo32, *band_len32;  // the FP32 convolution's bands
+    uint32_t *core_lo32, *core_len32;  // their cores (compensated m2 rows)
     double *w64;
     float *w32, *w32lo;  // FP32 weights and their remainders
     double *stats;
@@ -400,6 +411,10 @@ constexpr double kDefaultCutoff = 80.0;
 // the FP32 convolution uses the rows whose weights are >= e^-30 x the mode's
 // (the rest sum to < 1e-13)
 constexpr double kConvF32Cutoff = 30.0;
+// m2's compensated products cover the rows whose weights are >= e^-8 x the
+// mode's (+-4 standard deviations); the rest of the band holds < 1e-4 of the
+// weight and is summed in plain FP32
+constexpr double kConvCoreCutoff = 8.0;
 constexpr uint64_t kM4HighFreeNodes = 115001;  // max_s s^3 (N - s) < 2^64 for N <= 115,000
 
 // A second stream per device on which nz_ensemble runs the consumers of each
@@ -513,6 +528,8 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     L.w32lo = c.take<float>((size_t)P * L.cap);
     L.band_lo32 = c.take<uint32_t>(P);
     L.band_len32 = c.take<uint32_t>(P);
+    L.core_lo32 = c.take<uint32_t>(P);
+    L.core_len32 = c.take<uint32_t>(P);
     L.stats = c.take<double>((size_t)n_runs * P * 7);
     L.slices = n_runs < 1024 ? 1 : (n_runs < 65536 ? 16 : 64);
     L.part = c.take<double>((size_t)L.slices * P * 7 * 3);
@@ -558,7 +575,8 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         launch_binomial_weights(M, ps, P, cutoff, L.cap, L.band_lo, L.band_len, L.w64, nullptr, s);
         if (conv_precision != 0)
             launch_narrow_weights_f32(L.w64, L.band_lo, L.band_len, P, L.cap, exp(-fmin(cutoff, kConvF32Cutoff)),
-                                      L.w32, L.w32lo, L.band_lo32, L.band_len32, s);
+                                      exp(-kConvCoreCutoff), L.w32, L.w32lo, L.band_lo32, L.band_len32,
+                                      L.core_lo32, L.core_len32, s);
         if (cudaMemsetAsync(L.flag, 0, 4 * sizeof(uint32_t), s) != cudaSuccess) return NZ_ERR_CUDA;
         launch_init_runs(g, n_runs, L.nodes, L.state, L.flag, s);
         if (cudaMemsetAsync(L.stats, 0, sizeof(double) * (size_t)n_runs * P * 7, s) != cudaSuccess)
@@ -593,6 +611,8 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.w64 = L.w64;
     cp.w32 = L.w32;
     cp.w32lo = L.w32lo;
+    cp.core_lo = L.core_lo32;
+    cp.core_len = L.core_len32;
     cp.acc = L.stats;
     cp.errors = L.flag + 1;  // with the union-find's corruption count
     MicroParams mp;

@@ -222,6 +222,46 @@ void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, co
 }
 
 // =====================================================================
+// Classic canonical averages: binomial weights times microcanonical arrays
+// =====================================================================
+// out[i][c] = sum_j w[i][j] V[lo_i + j][c] for the band of p_i (FP64): the
+// sums percolate/percolate.py:1171-1221 (canonical_averages) forms with the
+// full-length pmf, over the rows where the pmf does not underflow.  One CTA
+// per (p, group of 32 columns): lane c of every warp owns column c (a row
+// of V is one coalesced load per warp), warps stride over the band's rows,
+// and the warps' partial sums are added in a fixed order (deterministic).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) band_dot_kernel(const uint32_t *band_lo, const uint32_t *band_len,
+                                                         const double *w, int32_t cap, const double *V,
+                                                         uint32_t rows, int32_t cols, double *out) {
+    __shared__ double part[BLOCK / 32][32];
+    const int pi = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.y * 32 + lane;
+    const uint32_t lo = band_lo[pi];
+    uint32_t len = min(band_len[pi], (uint32_t)cap);
+    if (lo >= rows) len = 0;
+    else len = min(len, rows - lo);
+    const double *wp = w + (size_t)pi * cap;
+    double acc = 0.0;
+    if (c < cols)
+        for (uint32_t j = warp; j < len; j += BLOCK / 32) acc = fma(wp[j], V[(size_t)(lo + j) * cols + c], acc);
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0 && c < cols) {
+        double t = 0.0;
+        for (int k = 0; k < BLOCK / 32; ++k) t += part[k][lane];
+        out[(size_t)pi * cols + c] = t;
+    }
+}
+
+void launch_band_dot(const uint32_t *band_lo, const uint32_t *band_len, const double *w, int32_t cap, int32_t P,
+                     const double *V, uint32_t rows, int32_t cols, double *out, cudaStream_t s) {
+    if (P <= 0 || cols <= 0) return;
+    dim3 g(P, (cols + 31) / 32);
+    band_dot_kernel<256><<<g, 256, 0, s>>>(band_lo, band_len, w, cap, V, rows, cols, out);
+}
+
+// =====================================================================
 // Banded convolution of record windows (ensemble path)
 // =====================================================================
 #ifndef NZ_CONV_PT
@@ -456,22 +496,41 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
 //   q = qh + ql        (qh = q rounded toward zero to 24 bits, ql = q - qh,
 //                       both exact in FP32 for q < 2^48)
 //   ph = wh qh, eh = fma(wh, qh, -ph)     (TwoProduct: ph + eh = wh qh exactly)
-//   (s, e) = TwoSum(s, ph)                (s + e = old s + ph exactly)
+//   (s, e) = Fast2Sum(max(s, ph), min(s, ph))  (s + e = old s + ph exactly)
 //   c += e + eh + wh ql + wl qh           (wl ql, ~2^-48 of the term, dropped)
 // The run's value is s + c (FP64), about 2^-44 relative; the statistic's
 // curve then inherits FP64-level accuracy from the FP64 run reduction.
+// Only the band's core -- the rows whose weight is >= e^-8 of the mode, +-4
+// standard deviations -- needs this: the tails hold < 1e-4 of the weight,
+// and plain FP32 products summed per chunk keep their error near 1e-11 of
+// the value.  Chunks of rows outside every core of a tile (about a third of
+// a tile's rows) take the plain path.
 struct Dot2Acc {
-    float s = 0.0f, c = 0.0f;
+    float s = 0.0f, c = 0.0f, tail = 0.0f;
+    // a compensated term.  Every term and the running sum are >= 0, so
+    // ordering the two operands by size (max / min, on the integer pipe)
+    // makes Dekker's Fast2Sum exact: 3 additions instead of TwoSum's 6.
     __device__ __forceinline__ void add(float wh, float wl, float qh, float ql) {
         const float ph = __fmul_rn(wh, qh);
         const float eh = __fmaf_rn(wh, qh, -ph);
-        const float t = __fadd_rn(s, ph);
-        const float bp = __fsub_rn(t, s);
-        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+        const float a = fmaxf(s, ph), b = fminf(s, ph);
+        const float t = __fadd_rn(a, b);
+        const float e = __fsub_rn(b, __fsub_rn(t, a));
         s = t;
         c = __fadd_rn(c, __fadd_rn(e, eh));
         c = __fmaf_rn(wh, ql, c);
         c = __fmaf_rn(wl, qh, c);
+    }
+    // a term of a chunk outside every core: plain FP32 product and sum,
+    // added into the running sum once per chunk by Fast2Sum (so the
+    // compensation stays of the size of the rounding errors it collects)
+    __device__ __forceinline__ void add_tail(float wh, float q) { tail = __fmaf_rn(wh, q, tail); }
+    __device__ __forceinline__ void flush_tail() {
+        const float a = fmaxf(s, tail), b = fminf(s, tail);
+        const float t = __fadd_rn(a, b);
+        c = __fadd_rn(c, __fsub_rn(b, __fsub_rn(t, a)));
+        s = t;
+        tail = 0.0f;
     }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
@@ -486,23 +545,36 @@ __device__ __forceinline__ void split_u32(uint32_t q, float &qh, float &ql) {
     ql = (float)(int32_t)(q - (uint32_t)qh);
 }
 
-// grid (run tiles, p tiles): each thread the kConvPT m2 values of its run
+// 16 probabilities per CTA: each loaded record feeds twice the compensated
+// arithmetic of an 8-probability tile
+#ifndef NZ_M2_PT
+#define NZ_M2_PT 16
+#endif
+constexpr int kM2PT = NZ_M2_PT;  // probabilities per CTA of the compensated m2 kernel
+
+// grid (run tiles, tiles of kM2PT probabilities): each thread the kM2PT m2
+// values of its run.  A chunk of rows that meets the core of any of the
+// tile's probabilities runs the compensated arithmetic on all its rows
+// (branch-free, so the kM2PT accumulator chains interleave); a chunk
+// entirely in the tails runs plain FP32 products.
 template <bool NARROW>
 __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
-    __shared__ float s_wh[kConvChunk][kConvPT], s_wl[kConvChunk][kConvPT];
-    __shared__ uint32_t s_lo[kConvPT], s_len[kConvPT];
+    __shared__ float s_wh[kConvChunk][kM2PT], s_wl[kConvChunk][kM2PT];
+    __shared__ uint32_t s_lo[kM2PT], s_len[kM2PT], s_clo[kM2PT], s_clen[kM2PT];
     __shared__ uint32_t s_range[2];
     const int r = blockIdx.x * kConvRuns + threadIdx.x;
-    const int p0 = blockIdx.y * kConvPT;
-    if (threadIdx.x < kConvPT) {
+    const int p0 = blockIdx.y * kM2PT;
+    if (threadIdx.x < kM2PT) {
         const int pi = p0 + threadIdx.x;
         s_lo[threadIdx.x] = pi < p.P ? p.band_lo[pi] : 0u;
         s_len[threadIdx.x] = pi < p.P ? p.band_len[pi] : 0u;
+        s_clo[threadIdx.x] = pi < p.P ? p.core_lo[pi] : 0u;
+        s_clen[threadIdx.x] = pi < p.P ? p.core_len[pi] : 0u;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t a = 0xffffffffu, b = 0;
-        for (int j = 0; j < kConvPT; ++j)
+        for (int j = 0; j < kM2PT; ++j)
             if (s_len[j]) { a = min(a, s_lo[j]); b = max(b, s_lo[j] + s_len[j]); }
         s_range[0] = max(a, p.n_begin);
         s_range[1] = min(b, p.n_end);
@@ -510,52 +582,81 @@ __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
     __syncthreads();
     const uint32_t nlo = s_range[0], nhi = s_range[1];
     if (nlo >= nhi) return;
-    Dot2Acc acc[kConvPT];
+    Dot2Acc acc[kM2PT];
     const uint32_t *m2n = reinterpret_cast<const uint32_t *>(p.rec.m2);
     for (uint32_t c0 = nlo; c0 < nhi; c0 += kConvChunk) {
         const uint32_t cn = min((uint32_t)kConvChunk, nhi - c0);
+        // does the chunk meet a core?  (uniform over the CTA)
+        bool core = false;
+#pragma unroll
+        for (int j = 0; j < kM2PT; ++j)
+            core |= s_clen[j] && s_clo[j] < c0 + cn && c0 < s_clo[j] + s_clen[j];
         __syncthreads();
-        for (int i = threadIdx.x; i < kConvChunk * kConvPT; i += kConvRuns) {
-            const int row = i / kConvPT, j = i % kConvPT;
-            const uint32_t n = c0 + row;
+        for (int i = threadIdx.x; i < kConvChunk * kM2PT; i += kConvRuns) {
+            const int rw = i / kM2PT, j = i % kM2PT;
+            const uint32_t n = c0 + rw;
             float vh = 0.0f, vl = 0.0f;
-            if (row < (int)cn && n >= s_lo[j] && n < s_lo[j] + s_len[j]) {
+            if (rw < (int)cn && n >= s_lo[j] && n < s_lo[j] + s_len[j]) {
                 const size_t widx = (size_t)(p0 + j) * p.cap + (n - s_lo[j]);
                 vh = p.w32[widx];
                 vl = p.w32lo[widx];
             }
-            s_wh[row][j] = vh;
-            s_wl[row][j] = vl;
+            s_wh[rw][j] = vh;
+            s_wl[rw][j] = vl;
         }
         __syncthreads();
         if (r >= p.n_runs) continue;
         const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
-        uint32_t i = 0;
-        for (; i + kConvBatch <= cn; i += kConvBatch) {
-            float qh[kConvBatch], ql[kConvBatch];
-#pragma unroll
-            for (int b = 0; b < kConvBatch; ++b) {
-                const size_t off = base + (size_t)(i + b) * p.rec.run_stride;
-                if (NARROW) split_u32(m2n[off], qh[b], ql[b]);
-                else split_u64(p.rec.m2[off], qh[b], ql[b]);
-            }
-#pragma unroll
-            for (int b = 0; b < kConvBatch; ++b)
-#pragma unroll
-                for (int j = 0; j < kConvPT; ++j) acc[j].add(s_wh[i + b][j], s_wl[i + b][j], qh[b], ql[b]);
-        }
-        for (; i < cn; ++i) {
+        auto load = [&](uint32_t i, float &qh, float &ql) {
             const size_t off = base + (size_t)i * p.rec.run_stride;
-            float qh, ql;
             if (NARROW) split_u32(m2n[off], qh, ql);
             else split_u64(p.rec.m2[off], qh, ql);
+        };
+        uint32_t i = 0;
+        if (core) {
+            for (; i + kConvBatch <= cn; i += kConvBatch) {
+                float qh[kConvBatch], ql[kConvBatch];
 #pragma unroll
-            for (int j = 0; j < kConvPT; ++j) acc[j].add(s_wh[i][j], s_wl[i][j], qh, ql);
+                for (int b = 0; b < kConvBatch; ++b) load(i + b, qh[b], ql[b]);
+#pragma unroll
+                for (int b = 0; b < kConvBatch; ++b)
+#pragma unroll
+                    for (int j = 0; j < kM2PT; ++j) acc[j].add(s_wh[i + b][j], s_wl[i + b][j], qh[b], ql[b]);
+            }
+            for (; i < cn; ++i) {
+                float qh, ql;
+                load(i, qh, ql);
+#pragma unroll
+                for (int j = 0; j < kM2PT; ++j) acc[j].add(s_wh[i][j], s_wl[i][j], qh, ql);
+            }
+        } else {
+            for (; i + kConvBatch <= cn; i += kConvBatch) {
+                float q[kConvBatch];
+#pragma unroll
+                for (int b = 0; b < kConvBatch; ++b) {
+                    float qh, ql;
+                    load(i + b, qh, ql);
+                    q[b] = __fadd_rn(qh, ql);
+                }
+#pragma unroll
+                for (int b = 0; b < kConvBatch; ++b)
+#pragma unroll
+                    for (int j = 0; j < kM2PT; ++j) acc[j].add_tail(s_wh[i + b][j], q[b]);
+            }
+            for (; i < cn; ++i) {
+                float qh, ql;
+                load(i, qh, ql);
+                const float q = __fadd_rn(qh, ql);
+#pragma unroll
+                for (int j = 0; j < kM2PT; ++j) acc[j].add_tail(s_wh[i][j], q);
+            }
+#pragma unroll
+            for (int j = 0; j < kM2PT; ++j) acc[j].flush_tail();
         }
     }
     if (r < p.n_runs) {
 #pragma unroll
-        for (int j = 0; j < kConvPT; ++j) {
+        for (int j = 0; j < kM2PT; ++j) {
             const int pi = p0 + j;
             if (pi >= p.P) continue;
             p.acc[((size_t)r * p.P + pi) * 7 + 4] += acc[j].value();
@@ -565,7 +666,7 @@ __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
 
 void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
-    dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
+    dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kM2PT - 1) / kM2PT, 1);
     if (p.rec.narrow) conv_m2_comp_kernel<true><<<g, kConvRuns, 0, s>>>(p);
     else conv_m2_comp_kernel<false><<<g, kConvRuns, 0, s>>>(p);
 }
@@ -615,10 +716,11 @@ void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double *w64, const uint32_t *band_lo,
                                                                    const uint32_t *band_len, int32_t cap, double rel,
-                                                                   float *w32, float *w32lo, uint32_t *lo32,
-                                                                   uint32_t *len32) {
+                                                                   double rel_core, float *w32, float *w32lo,
+                                                                   uint32_t *lo32, uint32_t *len32,
+                                                                   uint32_t *core_lo, uint32_t *core_len) {
     __shared__ double s_max[BLOCK / 32];
-    __shared__ uint32_t s_a[BLOCK / 32], s_b[BLOCK / 32];
+    __shared__ uint32_t s_a[BLOCK / 32], s_b[BLOCK / 32], s_ca[BLOCK / 32], s_cb[BLOCK / 32];
     const int pi = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double *w = w64 + (size_t)pi * cap;
     const uint32_t len = min(band_len[pi], (uint32_t)cap);
@@ -629,20 +731,33 @@ __global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double 
     __syncthreads();
     m = s_max[0];
     for (int k = 1; k < BLOCK / 32; ++k) m = fmax(m, s_max[k]);
-    const double thr = m * rel;
-    uint32_t a = 0xffffffffu, b = 0;
-    for (uint32_t j = threadIdx.x; j < len; j += BLOCK)
+    const double thr = m * rel, thr_core = m * rel_core;
+    uint32_t a = 0xffffffffu, b = 0, ca = 0xffffffffu, cb = 0;
+    for (uint32_t j = threadIdx.x; j < len; j += BLOCK) {
         if (w[j] >= thr) { a = min(a, j); b = max(b, j + 1); }
+        if (w[j] >= thr_core) { ca = min(ca, j); cb = max(cb, j + 1); }
+    }
     for (int o = 16; o > 0; o >>= 1) {
         a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
         b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+        ca = min(ca, __shfl_xor_sync(0xffffffffu, ca, o));
+        cb = max(cb, __shfl_xor_sync(0xffffffffu, cb, o));
     }
-    if (lane == 0) { s_a[warp] = a; s_b[warp] = b; }
+    if (lane == 0) { s_a[warp] = a; s_b[warp] = b; s_ca[warp] = ca; s_cb[warp] = cb; }
     __syncthreads();
-    a = s_a[0]; b = s_b[0];
-    for (int k = 1; k < BLOCK / 32; ++k) { a = min(a, s_a[k]); b = max(b, s_b[k]); }
+    a = s_a[0]; b = s_b[0]; ca = s_ca[0]; cb = s_cb[0];
+    for (int k = 1; k < BLOCK / 32; ++k) {
+        a = min(a, s_a[k]); b = max(b, s_b[k]);
+        ca = min(ca, s_ca[k]); cb = max(cb, s_cb[k]);
+    }
     if (b <= a) a = b = 0;  // an empty band stays empty
-    if (threadIdx.x == 0) { lo32[pi] = band_lo[pi] + a; len32[pi] = b - a; }
+    if (cb <= ca) ca = cb = 0;
+    if (threadIdx.x == 0) {
+        lo32[pi] = band_lo[pi] + a;
+        len32[pi] = b - a;
+        core_lo[pi] = band_lo[pi] + ca;
+        core_len[pi] = cb - ca;
+    }
     float *o = w32 + (size_t)pi * cap;
     float *ol = w32lo + (size_t)pi * cap;
     for (uint32_t j = threadIdx.x; j < (uint32_t)cap; j += BLOCK) {
@@ -654,10 +769,11 @@ __global__ void __launch_bounds__(BLOCK) narrow_weights_f32_kernel(const double 
 }
 
 void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
-                               int32_t cap, double rel, float *w32, float *w32lo, uint32_t *lo32, uint32_t *len32,
-                               cudaStream_t s) {
+                               int32_t cap, double rel, double rel_core, float *w32, float *w32lo, uint32_t *lo32,
+                               uint32_t *len32, uint32_t *core_lo, uint32_t *core_len, cudaStream_t s) {
     if (P <= 0) return;
-    narrow_weights_f32_kernel<256><<<P, 256, 0, s>>>(w64, band_lo, band_len, cap, rel, w32, w32lo, lo32, len32);
+    narrow_weights_f32_kernel<256><<<P, 256, 0, s>>>(w64, band_lo, band_len, cap, rel, rel_core, w32, w32lo, lo32,
+                                                     len32, core_lo, core_len);
 }
 
 // =====================================================================

@@ -29,6 +29,7 @@
 #include "nz_common.cuh"
 #include "nz_internal.cuh"
 #include "nz_records.cuh"
+#include "nz_tc.cuh"
 
 namespace nz {
 namespace {
@@ -45,7 +46,6 @@ static_assert(kTcK == 16 || kTcK == 32, "chunk of 16 or 32 rows");
 constexpr uint32_t kTcCols = 2 * kTcP;                // TMEM columns: two FP32 accumulators
 constexpr uint32_t kCoreBytes = 128;                  // core matrix: 8 rows x 16 bytes
 constexpr uint32_t kSbo = (kTcK / 4) * kCoreBytes;    // between 8-row groups
-constexpr uint64_t kWaitNs = 1000000000ull;           // mbarrier waits give up after 1 s
 
 struct TcShared {
     float a[2][2][kTcRuns * kTcK];  // [stage][hi, lo] records
@@ -62,74 +62,23 @@ struct TcShared {
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTcP >> 3) << 17) |
                             ((uint32_t)(kTcRuns >> 4) << 24);
 
-__device__ __forceinline__ uint32_t smem_u32(const void *ptr) {
-    return (uint32_t)__cvta_generic_to_shared(ptr);
-}
+using tc::fence_async_smem;
+using tc::mbar_wait;
+using tc::mma_commit;
+using tc::smem_u32;
+using tc::tmem_ld32;
+__device__ __forceinline__ void tc_fence_before() { tc::fence_before(); }
+__device__ __forceinline__ void tc_fence_after() { tc::fence_after(); }
 
-// Shared-memory matrix descriptor, no swizzle, K-major: start address >> 4
-// (bits 0-13), leading byte offset >> 4 = between core matrices adjacent in
-// K (bits 16-29), stride byte offset >> 4 = between 8-row groups (bits
-// 32-45), fixed 0b001 at bits 46-48, base offset 0, swizzle mode 0.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(kCoreBytes >> 4) << 16) |
-           ((uint64_t)(kSbo >> 4) << 32) | (1ull << 46);
-}
+// descriptor of one operand stage: core matrices adjacent in K 128 bytes
+// apart, 8-row groups kSbo apart
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::smem_desc(addr, kCoreBytes, kSbo); }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
         ::"r"(d), "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// generic-proxy shared-memory writes visible to the tensor cores
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Waits for the phase of the given parity; false after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    const uint64_t t0 = global_ns();
-    for (;;) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
-    }
-}
-
-// 32 consecutive FP32 columns of this warp's 32 TMEM lanes (lane = thread);
-// the load and its wait in one statement, so no use moves above the wait.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ float to_tf32(float x) {
@@ -205,15 +154,12 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     const int r = blockIdx.x * kTcRuns + t;
     const bool live = r < p.n_runs;
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sh.tmem)),
-                     "r"(kTcCols)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tc::tmem_alloc(smem_u32(&sh.tmem), kTcCols);
     }
     if (t == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh.mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&sh.mbar[1])) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        tc::mbar_init(smem_u32(&sh.mbar[0]));
+        tc::mbar_init(smem_u32(&sh.mbar[1]));
+        tc::mbar_init_fence();
     }
     tc_fence_before();
     __syncthreads();
@@ -333,7 +279,7 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     const bool any_bad = __syncthreads_or(bad);
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+        tc::tmem_dealloc(tmem, kTcCols);
     }
     if (any_bad) {
         if (t == 0 && p.errors) atomicAdd(p.errors, 1u);

@@ -47,6 +47,9 @@ void launch_binomial_weights(uint32_t M, const double *ps, int32_t P, double cut
                              uint32_t *band_lo, uint32_t *band_len, double *w, int32_t *overflow,
                              cudaStream_t s);
 void launch_binomial_pmf(uint32_t M, const double *ps, int32_t P, double cutoff, double *out, cudaStream_t s);
+// out[i * cols + c] = sum over the band of p_i of w[i][j] V[(lo_i + j) * cols + c] (FP64)
+void launch_band_dot(const uint32_t *band_lo, const uint32_t *band_len, const double *w, int32_t cap, int32_t P,
+                     const double *V, uint32_t rows, int32_t cols, double *out, cudaStream_t s);
 void launch_canonical_rows(const uint8_t *rows, uint32_t M, int32_t spanning, const double *factors,
                            int32_t n_sets, double *out, cudaStream_t s);
 
@@ -61,6 +64,7 @@ struct ConvParams {
     const double *w64;       // [P][cap]
     const float *w32;        // [P][cap] (FP32 path, its own narrower bands)
     const float *w32lo;      // [P][cap] w64 - w32 as FP32 (the compensated m2 products)
+    const uint32_t *core_lo, *core_len;  // rows whose weight is >= e^-8 of the mode (m2 compensated)
     double *acc;             // [n_runs][P][7], accumulated (+=)
     uint32_t *errors;        // tensor-core path: counts CTAs whose waits gave up (or null)
 };
@@ -71,10 +75,11 @@ bool conv_tc_grid_fits(int32_t n_runs, int32_t P);
 int launch_conv_window_tc(const ConvParams &p, cudaStream_t s);
 // FP32 weights of the rows where each band's weight is >= rel x its largest,
 // re-based at lo32 (the convolution's FP32 band)
-// (and their FP32 remainders w64 - w32 in w32lo)
+// (and their FP32 remainders w64 - w32 in w32lo), and the core rows whose
+// weight is >= rel_core x the largest
 void launch_narrow_weights_f32(const double *w64, const uint32_t *band_lo, const uint32_t *band_len, int32_t P,
-                               int32_t cap, double rel, float *w32, float *w32lo, uint32_t *lo32, uint32_t *len32,
-                               cudaStream_t s);
+                               int32_t cap, double rel, double rel_core, float *w32, float *w32lo, uint32_t *lo32,
+                               uint32_t *len32, uint32_t *core_lo, uint32_t *core_len, cudaStream_t s);
 // m2 (statistic 4) of the FP32 paths with compensated products and sums
 void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s);
 // part: scratch [slices][P*7][3] doubles

@@ -15,80 +15,183 @@
 
 #include "nz_common.cuh"
 #include "nz_internal.cuh"
+#include "nz_tc.cuh"
 
 namespace nz {
-
-__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float z) {
     return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
 }
 
-constexpr int kTile = 64;
-constexpr int kKc = 16;
+// ---------------------------------------------------------------------
+// GEMM on the tensor cores: tcgen05.mma kind::f16 with BF16 operands and an
+// FP32 accumulator in TMEM
+// ---------------------------------------------------------------------
+// C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]); A(m, k) = A[m * sam + k * sak]
+// (FP32, rounded to BF16 as it is staged), B(k, n) = B[k * sbk + n * sbn]
+// (BF16, or FP32 rounded to BF16).  epilogue 0: C = acc (+ bias); 1: Z = acc
+// + bias, C = GELU(Z).  accumulate: C += instead of C =.
+//
+// One CTA of 128 threads per 128 x ntile tile of C (ntile <= 128, a multiple
+// of 16): the threads stage 64-deep K chunks of A (128 rows) and B (ntile
+// rows) into shared memory as BF16 in the canonical no-swizzle K-major
+// layout (8-row x 16-byte core matrices, K-adjacent ones 128 bytes apart,
+// 8-row groups 1 KB apart), double-buffered; one thread issues four
+// 128 x ntile x 16 MMAs per chunk and commits them to the chunk's mbarrier;
+// thread t reads row t of the accumulator out of TMEM (tcgen05.ld, lane t)
+// for the epilogue.  Every mbarrier wait gives up after 1 s: the tile is
+// then written as NaN and counted in g_mlp_errors (nz_mlp_take_errors).
+constexpr int kGM = 128;   // rows of C per CTA (TMEM lanes)
+constexpr int kGK = 64;    // K per staged chunk: 4 MMAs of K = 16
+constexpr int kGN = 128;   // largest column tile
+constexpr uint32_t kGSbo = (kGK / 8) * tc::kCoreBytes;
 
-// C[m][n] = sum_k A(m, k) * B(k, n) (+ bias[n]); A(m, k) = A[m * sam + k * sak],
-// B(k, n) = Bm[k * sbk + n * sbn]; operands read as BF16-rounded FP32 (A) or
-// BF16 (B when b_bf16 != nullptr); FP32 accumulation.
-// epilogue 0: C = acc (+bias); 1: Z = acc + bias, C = GELU(Z) (Z stored).
-__global__ void __launch_bounds__(256) mlp_gemm_kernel(int M, int N, int K, const float *A, int sam, int sak,
+struct GemmSmem {
+    __nv_bfloat16 a[2][kGM * kGK];
+    __nv_bfloat16 b[2][kGN * kGK];
+    uint64_t mbar[2];
+    uint32_t tmem;
+};
+
+__device__ uint32_t g_mlp_errors;  // tiles whose mbarrier waits gave up
+
+// element (row, k) of a staged K-major operand, in BF16 units
+__device__ __forceinline__ int kmajor_idx(int row, int k) {
+    return (row >> 3) * (int)(kGSbo / 2) + (k >> 3) * 64 + (row & 7) * 8 + (k & 7);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t bf16_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kGM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__global__ void __launch_bounds__(kGM) mlp_gemm_kernel(int M, int N, int K, const float *A, int sam, int sak,
                                                        const float *Bf, const __nv_bfloat16 *Bh, int sbk, int sbn,
                                                        const float *bias, int epilogue, float *Z, float *C,
-                                                       int ldc, int accumulate) {
-    __shared__ float sA[kKc][kTile + 1];
-    __shared__ float sB[kKc][kTile + 1];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kKc) {
-        for (int i = threadIdx.x; i < kKc * kTile; i += 256) {
-            const int kk = i / kTile, mm = i % kTile;
-            const int m = m0 + mm, k = k0 + kk;
-            sA[kk][mm] = (m < M && k < K) ? bf16r(A[(size_t)m * sam + (size_t)k * sak]) : 0.0f;
-            const int n = n0 + mm;
-            float b = 0.0f;
-            if (n < N && k < K) {
-                const size_t idx = (size_t)k * sbk + (size_t)n * sbn;
-                b = Bh ? __bfloat162float(Bh[idx]) : bf16r(Bf[idx]);
-            }
-            sB[kk][mm] = b;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kKc; ++kk) {
-            float a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) { a[i] = sA[kk][ty * 4 + i]; b[i] = sB[kk][tx * 4 + i]; }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-        }
-        __syncthreads();
+                                                       int ldc, int accumulate, int ntile) {
+    extern __shared__ __align__(1024) uint8_t gemm_smem[];
+    GemmSmem &sh = *reinterpret_cast<GemmSmem *>(gemm_smem);
+    const int t = threadIdx.x, warp = t >> 5;
+    const int m0 = blockIdx.y * kGM, n0 = blockIdx.x * ntile;
+    const uint32_t cols = ntile <= 32 ? 32u : (ntile <= 64 ? 64u : 128u);  // TMEM: power of two >= 32
+    if (warp == 0) tc::tmem_alloc(tc::smem_u32(&sh.tmem), cols);
+    if (t == 0) {
+        tc::mbar_init(tc::smem_u32(&sh.mbar[0]));
+        tc::mbar_init(tc::smem_u32(&sh.mbar[1]));
+        tc::mbar_init_fence();
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int m = m0 + ty * 4 + i;
-        if (m >= M) continue;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int n = n0 + tx * 4 + j;
-            if (n >= N) continue;
-            float v = acc[i][j] + (bias ? bias[n] : 0.0f);
-            const size_t o = (size_t)m * ldc + n;
-            if (epilogue == 1) { Z[o] = v; v = gelu(v); }
-            C[o] = accumulate ? C[o] + v : v;
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = sh.tmem;
+    const int nch = (K + kGK - 1) / kGK;
+    // thread index -> element: K fastest when K is the contiguous dimension
+    // of the source, else rows fastest (coalesced global loads either way)
+    const bool a_kfast = sak == 1, b_kfast = sbk == 1;
+    auto stage = [&](int c, int buf) {
+        const int k0 = c * kGK;
+        __nv_bfloat16 *sa = sh.a[buf], *sb = sh.b[buf];
+        for (int i = t; i < kGM * kGK; i += kGM) {
+            const int r = a_kfast ? i / kGK : i % kGM;
+            const int k = a_kfast ? i % kGK : i / kGM;
+            const int gm = m0 + r, gk = k0 + k;
+            const float v = (gm < M && gk < K) ? A[(size_t)gm * sam + (size_t)gk * sak] : 0.0f;
+            sa[kmajor_idx(r, k)] = __float2bfloat16_rn(v);
         }
+        for (int i = t; i < ntile * kGK; i += kGM) {
+            const int r = b_kfast ? i / kGK : i % ntile;
+            const int k = b_kfast ? i % kGK : i / ntile;
+            const int gn = n0 + r, gk = k0 + k;
+            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+            if (gn < N && gk < K) {
+                const size_t idx = (size_t)gk * sbk + (size_t)gn * sbn;
+                v = Bh ? Bh[idx] : __float2bfloat16_rn(Bf[idx]);
+            }
+            sb[kmajor_idx(r, k)] = v;
+        }
+    };
+    stage(0, 0);
+    bool bad = false;
+    int c = 0;
+    for (; c < nch; ++c) {
+        const int buf = c & 1;
+        tc::fence_async_smem();
+        tc::fence_before();
+        if (__syncthreads_or(bad)) break;  // a wait below gave up
+        if (t == 0) {
+            tc::fence_after();
+            const uint32_t a0 = tc::smem_u32(sh.a[buf]), b0 = tc::smem_u32(sh.b[buf]);
+#pragma unroll
+            for (int ks = 0; ks < kGK / 16; ++ks) {
+                const uint32_t o = (uint32_t)ks * 2 * tc::kCoreBytes;  // K = 16: two core matrices
+                mma_bf16(tmem, tc::smem_desc(a0 + o, tc::kCoreBytes, kGSbo),
+                         tc::smem_desc(b0 + o, tc::kCoreBytes, kGSbo), bf16_idesc(ntile),
+                         (c > 0 || ks > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(tc::smem_u32(&sh.mbar[buf]));
+        }
+        if (c + 1 < nch) {
+            // the other buffer is free once the MMAs of chunk c - 1 are done
+            if (c >= 1) bad = !tc::mbar_wait(tc::smem_u32(&sh.mbar[(c - 1) & 1]), ((c - 1) >> 1) & 1);
+            if (!bad) stage(c + 1, (c + 1) & 1);
+        }
+    }
+    // MMAs complete in order: the last chunk issued covers them all
+    if (c > 0 && !tc::mbar_wait(tc::smem_u32(&sh.mbar[(c - 1) & 1]), ((c - 1) >> 1) & 1)) bad = true;
+    tc::fence_before();
+    const bool any_bad = __syncthreads_or(bad) || c < nch;
+    tc::fence_after();
+    const int m = m0 + t;
+    if (!any_bad) {
+        for (int j0 = 0; j0 < ntile; j0 += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)j0, v);
+            if (m < M) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int n = n0 + j0 + j;
+                    if (j0 + j >= ntile || n >= N) continue;
+                    float x = v[j] + (bias ? bias[n] : 0.0f);
+                    const size_t o = (size_t)m * ldc + n;
+                    if (epilogue == 1) { Z[o] = x; x = gelu(x); }
+                    C[o] = accumulate ? C[o] + x : x;
+                }
+            }
+        }
+    } else {
+        if (m < M)
+            for (int j = 0; j < ntile && n0 + j < N; ++j) C[(size_t)m * ldc + n0 + j] = __int_as_float(0x7fc00000);
+        if (t == 0) atomicAdd(&g_mlp_errors, 1u);
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, cols);
     }
 }
 
 static void gemm(int M, int N, int K, const float *A, int sam, int sak, const float *Bf, const __nv_bfloat16 *Bh,
                  int sbk, int sbn, const float *bias, int epilogue, float *Z, float *C, int ldc, int accumulate,
                  cudaStream_t s) {
-    dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-    mlp_gemm_kernel<<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, Bf, Bh, sbk, sbn, bias, epilogue, Z, C, ldc,
-                                         accumulate);
+    if (M <= 0 || N <= 0) return;
+    const int ntile = N >= kGN ? kGN : ((N + 15) / 16) * 16;
+    // above 48 KB of dynamic shared memory the launch needs the attribute,
+    // which belongs to the function in the current device's context
+    cudaFuncSetAttribute(mlp_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GemmSmem));
+    dim3 grid((N + ntile - 1) / ntile, (M + kGM - 1) / kGM);
+    mlp_gemm_kernel<<<grid, kGM, sizeof(GemmSmem), s>>>(M, N, K, A, sam, sak, Bf, Bh, sbk, sbn, bias, epilogue, Z,
+                                                         C, ldc, accumulate, ntile);
 }
 
 __global__ void to_bf16_kernel(const float *a, __nv_bfloat16 *b, int64_t n) {
@@ -259,6 +362,15 @@ int nz_mlp_backward(const int32_t *widths, int32_t n_layers, int32_t batch, cons
         gelu_back_kernel<<<blocks_for(cnt), 256, 0, s>>>(z + act_off[l - 1], dA, dZ, cnt);
     }
     return cudaGetLastError() == cudaSuccess ? NZ_OK : NZ_ERR_CUDA;
+}
+
+int nz_mlp_take_errors(uint32_t *count) {
+    if (!count) return NZ_ERR_INVALID;
+    const uint32_t zero = 0;
+    if (cudaMemcpyFromSymbol(count, g_mlp_errors, sizeof(uint32_t)) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_mlp_errors, &zero, sizeof(uint32_t)) != cudaSuccess)
+        return NZ_ERR_CUDA;
+    return NZ_OK;
 }
 
 int nz_mlp_adam(float *params, const float *grads, float *m, float *v, void *params_bf16, int64_t count,

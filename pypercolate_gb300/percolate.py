@@ -411,19 +411,36 @@ def microcanonical_averages_arrays(microcanonical_averages):
 def canonical_averages(ps, microcanonical_averages_arrays):
     """Canonical averages at each p: binomial weights (FP64, GPU) times every
     microcanonical array, confidence bounds included, as the reference does
-    (percolate/percolate.py:1112-1221); one FP64 GEMM on the GPU."""
+    (percolate/percolate.py:1112-1221).  The weights are computed over the
+    band where the pmf does not underflow (nz_binomial_weights, cutoff 745)
+    and contracted with the arrays by nz_band_dot (FP64, one CTA per p)."""
     torch = nat.torch_cuda()
+    lib = nat.lib_handle()
     arr = microcanonical_averages_arrays
     N, M = arr['N'], arr['M']
     ps = np.asarray(ps, dtype=np.float64)
+    flat = np.ascontiguousarray(ps.ravel())
+    P = flat.size
     spanning = 'spanning_cluster' in arr
     cols = [arr['max_cluster_size'][:, None], arr['max_cluster_size_ci'],
             arr['moments'].T, arr['moments_ci'].transpose(1, 0, 2).reshape(M + 1, 10)]
     if spanning:
         cols += [arr['spanning_cluster'][:, None], arr['spanning_cluster_ci']]
-    V = torch.from_numpy(np.ascontiguousarray(np.hstack(cols))).cuda()
-    W = torch.from_numpy(binomial_pmfs(M, ps.ravel())).cuda()
-    C = (W @ V).cpu().numpy()
+    V = torch.from_numpy(np.ascontiguousarray(np.hstack(cols), dtype=np.float64)).cuda()
+    ncols = int(V.shape[1])
+    cutoff = 745.0  # FP64 underflow: the range of the reference's pmf
+    cap = int(lib.nz_binomial_band_cap(M, cutoff))
+    d_ps = torch.from_numpy(flat.copy()).cuda()
+    lo = torch.empty(P, dtype=torch.int32, device='cuda')
+    ln = torch.empty(P, dtype=torch.int32, device='cuda')
+    w = torch.empty(P * cap, dtype=torch.float64, device='cuda')
+    s = nat.stream_handle()
+    nat.check(lib.nz_binomial_weights(M, nat.ptr(d_ps), P, cutoff, cap, nat.ptr(lo), nat.ptr(ln),
+                                      nat.ptr(w), s), 'nz_binomial_weights')
+    out = torch.empty(P * ncols, dtype=torch.float64, device='cuda')
+    nat.check(lib.nz_band_dot(nat.ptr(lo), nat.ptr(ln), nat.ptr(w), cap, P, nat.ptr(V), M + 1,
+                              ncols, nat.ptr(out), s), 'nz_band_dot')
+    C = out.cpu().numpy().reshape(P, ncols)
     ret = {'ps': ps, 'N': N, 'M': M}
     ret['max_cluster_size'] = C[:, 0]
     ret['max_cluster_size_ci'] = C[:, 1:3]

@@ -164,6 +164,15 @@ class MLP:
             nat.ptr(self.params_bf16), self.count, lr, beta1, beta2, eps, self.step_count,
             nat.stream_handle()), 'nz_mlp_adam')
 
+    @staticmethod
+    def take_errors():
+        """Tensor-core GEMM tiles whose waits gave up since the last call
+        (0 in every valid use; such tiles hold NaN)."""
+        import ctypes
+        v = ctypes.c_uint32(0)
+        nat.check(nat.lib_handle().nz_mlp_take_errors(ctypes.byref(v)), 'nz_mlp_take_errors')
+        return int(v.value)
+
     def fit(self, X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, log_every=0, decay=0.0):
         """Standardise, then Adam on random mini-batches; the learning rate
         stays `lr`, then (decay > 0) falls geometrically to lr * decay over
@@ -189,6 +198,8 @@ class MLP:
             self.adam(rate)
             if log_every and (k % log_every == 0 or k == steps - 1):
                 trace.append((k, float(loss)))
+        if self.take_errors():
+            raise RuntimeError('MLP tensor-core GEMM waits gave up during training')
         return trace
 
     def predict(self, X):

@@ -21,43 +21,39 @@ def test_shard_runs_partition():
         shard_runs(10, 2, 2)
 
 
-def _rank_rows(oracle, hpc, L, key, run0, count, ps):
-    """Canonical-averages rows of `count` oracle runs (CPU stand-in for one
-    rank's GPU ensemble)."""
-    M = 2 * L * (L - 1)
+def _rank_state(oracle, L, key, run0, count, ps):
+    """One rank's ensemble state (the dict Ensemble.state() returns:
+    canonical (count, mean, M2) per (p, statistic), exact microcanonical
+    accumulators, ledger) for `count` oracle runs -- a CPU stand-in for the
+    state of that rank's GPU ensemble."""
+    N, M = L * L, 2 * L * (L - 1)
     W = np.stack([oracle.binomial_pmf(M, p) for p in ps])
     acc = None
-    for r in range(run0, run0 + count):
-        q = oracle.q_matrix(oracle.lattice_run(oracle.GRID_2D, L,
-                                               oracle.philox_permutation(key, r, M)))
-        row = (1.0, W @ q, np.zeros((len(ps), 7)))
+    vals = np.zeros((6, count, M + 1), dtype=object)
+    span = np.zeros(M + 1, dtype=np.int64)
+    for i, r in enumerate(range(run0, run0 + count)):
+        run = oracle.lattice_run(oracle.GRID_2D, L, oracle.philox_permutation(key, r, M))
+        row = (1.0, W @ oracle.q_matrix(run), np.zeros((len(ps), 7)))
         acc = row if acc is None else oracle.reduce_rows(acc, row)
+        exact = run['moments_u64'].astype(object) + run['moments_hi'].astype(object) * (1 << 64)
+        mx = run['max'].astype(object)
+        for k, v in enumerate((mx, exact[:, 0], N - mx, exact[:, 2], exact[:, 3], exact[:, 4])):
+            vals[k, i] = v
+        span += run['span']
     n, mean, m2 = acc
-    out = np.empty(len(ps), dtype=hpc.canonical_averages_dtype(True))
-    out['number_of_runs'] = int(n)
-    out['percolation_probability_mean'] = mean[:, 0]
-    out['percolation_probability_m2'] = m2[:, 0]
-    out['max_cluster_size_mean'] = mean[:, 1]
-    out['max_cluster_size_m2'] = m2[:, 1]
-    out['moments_mean'] = mean[:, 2:]
-    out['moments_m2'] = m2[:, 2:]
-    return out
-
-
-def _oracle_reducer(a, b):
-    """bond_reduce restated on the CPU (test stand-in for the GPU kernel)."""
-    from oracle import oracle as O
-    out = a.copy()
-    na = a['number_of_runs'].astype(float)
-    nb = b['number_of_runs'].astype(float)
-    for key in ('percolation_probability', 'max_cluster_size', 'moments'):
-        ma, sa = a[key + '_mean'], a[key + '_m2']
-        mb, sb = b[key + '_mean'], b[key + '_m2']
-        shape = (-1,) + (1,) * (ma.ndim - 1)
-        _, m, s = O.reduce_rows((na.reshape(shape), ma, sa), (nb.reshape(shape), mb, sb))
-        out[key + '_mean'], out[key + '_m2'] = m, s
-    out['number_of_runs'] = a['number_of_runs'] + b['number_of_runs']
-    return out
+    sums = vals.sum(axis=1).reshape(-1)
+    fl = vals.astype(np.float64)
+    micro_m2 = ((fl - fl.mean(axis=1, keepdims=True)) ** 2).sum(axis=1).reshape(-1)
+    meta = {'kind': 'grid', 'model': 'bond', 'wrap': 'either', 'length': L, 'N': N, 'M': M,
+            'spanning': True, 'precision': 'fp64', 'window': 0, 'cutoff': 80.0, 'micro': True}
+    return {'meta': meta, 'ps': np.asarray(ps, np.float64),
+            'count': np.array([count], np.int64), 'mean': mean.reshape(-1),
+            'm2': m2.reshape(-1), 'ledger': np.array([[key, run0, count]], np.uint64),
+            'micro': {'count': np.array([count], np.int64), 'span_count': span,
+                      'sum_lo': np.array([int(v) & (2 ** 64 - 1) for v in sums],
+                                         np.uint64).view(np.int64),
+                      'sum_hi': np.array([int(v) >> 64 for v in sums], np.uint64).view(np.int64),
+                      'm2': micro_m2}}
 
 
 def _worker(rank, world, port, total, result_path):
@@ -65,17 +61,17 @@ def _worker(rank, world, port, total, result_path):
     sys.path.insert(0, REPO)
     import torch.distributed as dist
     from oracle import oracle as O
-    from pypercolate_gb300 import hpc
-    from pypercolate_gb300.distributed import gather_rows, merge_rows, shard_runs
+    from pypercolate_gb300 import store
+    from pypercolate_gb300.distributed import gather_objects, merge_states, shard_runs
     os.environ['MASTER_ADDR'] = '127.0.0.1'
     os.environ['MASTER_PORT'] = str(port)
     dist.init_process_group('gloo', rank=rank, world_size=world)
     ps = np.linspace(0.3, 0.7, 5)
     run0, count = shard_runs(total, world, rank)
-    rows = _rank_rows(O, hpc, 6, 77, run0, count, ps)
-    merged = merge_rows(gather_rows(rows), reducer=_oracle_reducer)
+    state = _rank_state(O, 6, 77, run0, count, ps)
+    merged = merge_states(gather_objects(state))
     if rank == 0:
-        np.save(result_path, merged)
+        store.save_state(result_path, merged)
     dist.barrier()
     dist.destroy_process_group()
 
@@ -89,17 +85,33 @@ def _free_port():
 
 
 def test_two_rank_merge_equals_single_process(tmp_path):
+    """Two gloo ranks each hold the state of their shard of runs; the
+    package's gather and host merge give the state of all runs in one
+    process: canonical means to 1e-12, M2 to 1e-9, exact micro sums and
+    spanning counts equal, the ledger covering every run once."""
     import torch.multiprocessing as mp
     from oracle import oracle as O
-    from pypercolate_gb300 import hpc
+    from pypercolate_gb300 import store
     total = 23
-    out = str(tmp_path / 'merged.npy')
+    out = str(tmp_path / 'merged.npz')
     mp.start_processes(_worker, args=(2, _free_port(), total, out), nprocs=2, join=True,
                        start_method='spawn')
-    merged = np.load(out)
-    single = _rank_rows(O, hpc, 6, 77, 0, total, np.linspace(0.3, 0.7, 5))
-    assert np.all(merged['number_of_runs'] == total)
-    for k in ('percolation_probability_mean', 'max_cluster_size_mean', 'moments_mean'):
-        np.testing.assert_allclose(merged[k], single[k], rtol=1e-12)
-    for k in ('percolation_probability_m2', 'max_cluster_size_m2', 'moments_m2'):
-        np.testing.assert_allclose(merged[k], single[k], rtol=1e-9, atol=1e-9)
+    merged = store.load_state(out)
+    single = _rank_state(O, 6, 77, 0, total, np.linspace(0.3, 0.7, 5))
+    assert int(merged['count'][0]) == total
+    assert store.ledger_runs(merged['ledger']) == total
+    np.testing.assert_allclose(merged['mean'], single['mean'], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(merged['m2'], single['m2'], rtol=1e-9, atol=1e-9)
+    for k in ('sum_lo', 'sum_hi', 'span_count', 'count'):
+        assert np.array_equal(merged['micro'][k], single['micro'][k]), k
+    np.testing.assert_allclose(merged['micro']['m2'], single['micro']['m2'], rtol=1e-9, atol=1e-6)
+
+
+def test_host_merge_refuses_shared_runs():
+    from oracle import oracle as O
+    from pypercolate_gb300.distributed import merge_states
+    ps = np.linspace(0.4, 0.6, 3)
+    a = _rank_state(O, 4, 5, 0, 3, ps)
+    b = _rank_state(O, 4, 5, 2, 3, ps)  # run 2 in both
+    with pytest.raises(ValueError):
+        merge_states([a, b])

@@ -115,3 +115,28 @@ def test_state_of_other_models_round_trips(gpu, tmp_path):
         if kw['model'] == 'site':
             with pytest.raises(ValueError):
                 loaded.merge(Ensemble(kw['kind'], kw['length'], PS, micro=kw['micro']))
+
+
+def test_host_merge_of_states_matches_device_merge(gpu):
+    """distributed.merge_states (numpy, for a coordinator without a GPU)
+    gives the device merge's result (Ensemble.merge: nz_canonical_merge,
+    nz_micro_merge): canonical and micro M2 to 1e-14, exact sums and counts
+    equal."""
+    from pypercolate_gb300.distributed import merge_states
+    shards = []
+    for run0, n in ((0, 200), (200, 150), (350, 77)):
+        e = make()
+        e.run(n, key=5, run0=run0)
+        shards.append(e)
+    states = [e.state() for e in shards]
+    dev = shards[0]
+    for e in shards[1:]:
+        dev.merge(e)
+    want = dev.state()
+    got = merge_states(states)
+    assert int(got['count'][0]) == int(want['count'][0]) == 427
+    np.testing.assert_allclose(got['mean'], want['mean'], rtol=1e-14, atol=1e-300)
+    np.testing.assert_allclose(got['m2'], want['m2'], rtol=1e-14, atol=1e-12)
+    for k in ('count', 'span_count', 'sum_lo', 'sum_hi'):
+        assert np.array_equal(np.asarray(got['micro'][k]), np.asarray(want['micro'][k])), k
+    np.testing.assert_allclose(got['micro']['m2'], want['micro']['m2'], rtol=1e-14, atol=1e-9)

@@ -117,43 +117,61 @@ def split_value(q):
 
 
 def dot2_add(s, c, wh, wl, qh, ql):
-    """One term of conv_m2_comp_kernel's compensated dot product (Dot2Acc)."""
+    """One compensated term of conv_m2_comp_kernel (Dot2Acc.add):
+    TwoProduct, and Fast2Sum on the operands ordered by size (all >= 0)."""
     ph = f32(wh * qh)
     eh = fmaf(wh, qh, -ph)
-    t = f32(s + ph)
-    bp = f32(t - s)
-    e = f32(f32(s - f32(t - bp)) + f32(ph - bp))
+    a, b = max(s, ph), min(s, ph)
+    t = f32(a + b)
+    e = f32(b - f32(t - a))
     c = f32(c + f32(e + eh))
     c = fmaf(wh, ql, c)
     c = fmaf(wl, qh, c)
     return t, c
 
 
-@pytest.mark.parametrize('L,rows', [(256, 800), (1024, 1500)])
+@pytest.mark.parametrize('L,rows', [(256, 2800), (1024, 3000)])
 def test_compensated_m2_products_reach_5e_11(L, rows):
-    """The m2 convolution of one run over a binomial band, with FP64
-    weights split into FP32 hi + lo and m2 values (up to N^2 / 4) split into
-    exact FP32 parts, comes within 5e-11 relative of the exact dot product
-    of the FP64 weights -- what the susceptibility curve needs to stay within
-    1e-6 absolute of FP64 at L = 1024 (m2 / N up to ~2e4) -- where plain FP32
-    products summed in FP32 are ~1e-7 off."""
+    """The m2 convolution of one run over a binomial-shaped band as
+    conv_m2_comp_kernel does it -- FP64 weights split into FP32 hi + lo, m2
+    values (up to N^2 / 4) split into exact FP32 parts, compensated products
+    and sums over every chunk of 128 rows that meets the core (weights >=
+    e^-8 of the largest), plain FP32 products over chunks entirely in the
+    tails, added into the running sum chunk by chunk -- comes within 5e-11
+    relative of the exact dot product of the FP64 weights: what the
+    susceptibility curve needs to stay within 1e-6 absolute of FP64 at
+    L = 1024 (m2 / N up to ~2e4).  Plain FP32 products summed in FP32 are
+    ~1e-7 off."""
     rng = np.random.default_rng(L)
     N = L * L
     n = np.arange(rows)
-    w = np.exp(-0.5 * ((n - rows / 2) / (rows / 9)) ** 2)
+    sigma = rows / 15.5  # the FP32 band: +-7.75 standard deviations
+    w = np.exp(-0.5 * ((n - rows / 2) / sigma) ** 2)
     w /= w.sum()
+    core = w >= w.max() * np.exp(-8.0)
     hi = rng.integers(1, N * N // 4, rows // 4 + 1)
     q = [int(x) for x in np.repeat(hi, 4)[:rows] + rng.integers(0, 1000, rows)]
     exact = sum(Fraction(float(wi)) * qi for wi, qi in zip(w, q))
     s = c = f32(0)
     plain = f32(0)
-    for wi, qi in zip(w, q):
-        wh = f32(wi)
-        wl = f32(float(wi) - float(wh))
-        qh, ql = split_value(qi)
-        assert int(qh) + int(ql) == qi
-        s, c = dot2_add(s, c, wh, wl, qh, ql)
-        plain = fmaf(wh, f32(qi), plain)
+    for c0 in range(0, rows, 128):  # chunks of 128 rows
+        compensated = bool(core[c0:c0 + 128].any())
+        tail = f32(0)
+        for i in range(c0, min(rows, c0 + 128)):
+            wi, qi = w[i], q[i]
+            wh = f32(wi)
+            wl = f32(float(wi) - float(wh))
+            qh, ql = split_value(qi)
+            assert int(qh) + int(ql) == qi
+            if compensated:
+                s, c = dot2_add(s, c, wh, wl, qh, ql)
+            else:
+                tail = fmaf(wh, f32(qh + ql), tail)
+            plain = fmaf(wh, f32(qi), plain)
+        if not compensated:  # flush_tail: Fast2Sum into the running sum
+            a, b = max(s, tail), min(s, tail)
+            t = f32(a + b)
+            c, s = f32(c + f32(b - f32(t - a))), t
     got = Fraction(float(s)) + Fraction(float(c))
     assert abs(got - exact) / exact < 5e-11
     assert abs(Fraction(float(plain)) - exact) / exact > 1e-9

@@ -167,6 +167,8 @@ def parse():
     ap.add_argument('--plain-runs', type=int, default=8192,
                     help='runs timed on the plain path (0: skip)')
     ap.add_argument('--plain-chunk', type=int, default=4096)
+    ap.add_argument('--no-tune', dest='tune', action='store_false',
+                    help='skip the launch-shape autotuner of the main leg (library defaults)')
     ap.add_argument('--no-plain-mix', dest='plain_mix', action='store_false',
                     help='skip the one-lattice-per-launch timing of the uneven workload')
     ap.add_argument('--curve-sample', type=int, default=2048,
@@ -479,8 +481,18 @@ def main():
         nat.set_l2_fetch_granularity(args.l2_fetch)
     l2_fetch = nat.get_l2_fetch_granularity()
     ps = np.linspace(0.0, 1.0, args.P)
+    # launch shapes from the autotuner, timed on this workload (before the
+    # main ensemble holds its workspace)
+    tuned = None
+    tuning, window = None, args.window
+    if args.tune:
+        from pypercolate_gb300.autotune import tune_ensemble
+        tuned = tune_ensemble(args.lattice, L, ps, R, precision=args.precision,
+                              micro=not args.no_micro, model=args.model, cache_path=None)
+        tuning = tuned['best']
+        window = window or tuning['window']
     ens = Ensemble(args.lattice, L, ps, precision=args.precision, micro=not args.no_micro,
-                   window=args.window, model=args.model)
+                   window=window, model=args.model, tuning=tuning)
     N, M = ens.N, ens.M  # M = number of steps (bonds, or sites for the site model)
     default_leg = args.lattice == 'grid' and args.model == 'bond'
     unit = 'bond additions/s' if args.model == 'bond' else 'site additions/s'
@@ -549,7 +561,7 @@ def main():
     curve_err = None
     if args.curve_sample > 0 and default_leg:
         curve_err = curve_errors_vs_fp64(L, ps, args.precision, min(args.curve_sample, R),
-                                         run_base + args.warmup * R, bench_window(M, R, args.window))
+                                         run_base + args.warmup * R, bench_window(M, R, window))
 
     # plain GPU path (one lattice per launch): chunks of runs whose records for
     # all M+1 rows are materialised by one union-find launch, then reduced
@@ -629,7 +641,7 @@ def main():
     t0 = time.perf_counter()
     for k in range(args.e2e_steps):
         e = Ensemble(args.lattice, L, h_ps.numpy(), precision=args.precision, model=args.model,
-                     micro=not args.no_micro, window=args.window)
+                     micro=not args.no_micro, window=window, tuning=tuning)
         e._ws = ens._ws  # reuse the device workspace
         e.d_ps.copy_(h_ps, non_blocking=True)
         e.run(R, key=KEY, run0=run_base + 10 ** 8 + k * R)
@@ -677,6 +689,10 @@ def main():
                             'plain': plain['union_find_only'] if plain else None},
         'curve_err_vs_fp64': curve_err,
         'clocks': clocks,
+        'autotune': ({'best': tuned['best'],
+                      'table': [[c, ms] for c, ms in tuned['table']],
+                      'candidates_ms': 'one ensemble step of the workload per candidate'}
+                     if tuned else None),
         'gpu_launches': gpu_launches,
         'merged_runs': merged_runs,
         'union_find_errors': uf_errors,

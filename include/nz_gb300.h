@@ -347,6 +347,30 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
                 double *acc_mean, double *acc_m2, const NzMicroAccum *micro,
                 void *stream);
 
+/* Launch shapes of the ensemble pipeline, chosen by an autotuner (the Python
+ * package's autotune.tune_ensemble) rather than fixed; a field of 0 takes the
+ * default.  uf_block: runs per CTA of the union-find (32, 64 or 128; 128);
+ * m2_tile: probabilities per CTA of the compensated m2 convolution (8 or 16;
+ * 16); reduce_slices: slices of runs of the canonical run reduction (1 ..
+ * 256; 1, 16 or 64 by run count).  The record window is nz_ensemble's
+ * `window`.  No counterpart in the reference (its runs are Python calls). */
+typedef struct NzTuning {
+    int32_t uf_block;
+    int32_t m2_tile;
+    int32_t reduce_slices;
+} NzTuning;
+/* nz_ensemble with explicit launch shapes (tuning may be NULL: defaults);
+ * results do not depend on them beyond the order of FP64 additions in the
+ * run reduction. */
+int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning,
+                      int32_t n_runs, uint64_t key, uint64_t run0,
+                      const double *ps, int32_t P, double cutoff,
+                      int32_t window, int32_t conv_precision,
+                      const NzTuning *tuning, void *workspace,
+                      size_t workspace_bytes, uint64_t *acc_count,
+                      double *acc_mean, double *acc_m2,
+                      const NzMicroAccum *micro, void *stream);
+
 /* ---- batched uneven ensembles (one persistent launch) ------------------ */
 /* Run r draws its substrate from Philox-4x32-10 (key, counter r): a chain
  * with probability chain_share / 2^32, else a square lattice; the length L

@@ -58,6 +58,11 @@ class NzMicroAccum(ctypes.Structure):
                 ('sum_hi', _vp), ('m2', _vp)]
 
 
+class NzTuning(ctypes.Structure):
+    _fields_ = [('uf_block', ctypes.c_int32), ('m2_tile', ctypes.c_int32),
+                ('reduce_slices', ctypes.c_int32)]
+
+
 class NzMixSpec(ctypes.Structure):
     _fields_ = [('grid_min', ctypes.c_uint32), ('grid_max', ctypes.c_uint32),
                 ('chain_min', ctypes.c_uint32), ('chain_max', ctypes.c_uint32),
@@ -155,6 +160,11 @@ _SIGNATURES = [
      [ctypes.POINTER(NzGraph), ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
       ctypes.c_uint64, _vp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
       ctypes.c_int32, _vp, ctypes.c_size_t, _vp, _vp, _vp,
+      ctypes.POINTER(NzMicroAccum), _vp]),
+    ('nz_ensemble_tuned', ctypes.c_int,
+     [ctypes.POINTER(NzGraph), ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64,
+      ctypes.c_uint64, _vp, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+      ctypes.c_int32, ctypes.POINTER(NzTuning), _vp, ctypes.c_size_t, _vp, _vp, _vp,
       ctypes.POINTER(NzMicroAccum), _vp]),
 ]
 

@@ -1,10 +1,18 @@
-"""Autotuner for the batched uneven ensembles (``nz_mix``).
+"""Autotuners for the two ensemble paths.
 
-Candidates are (persistent threads = runs in flight, threads per CTA,
-shared-memory node slot per thread = placement).  Each candidate runs the
-same workload on a sample of the runs, timed with CUDA events; the fastest
-wins.  Results are cached in a JSON file keyed by the GPU name and the
-workload, so later processes reuse the choice.
+tune_mix       batched uneven ensembles (``nz_mix``): persistent threads
+               (runs in flight), threads per CTA (runs per CTA) and the
+               shared-memory node slot per thread (placement: small lattices
+               in shared memory, the rest in HBM / L2).
+tune_ensemble  one lattice per ensemble (``nz_ensemble_tuned``): runs per
+               CTA of the union-find, the probability tile of the compensated
+               m2 convolution, the record window (rows reduced and convolved
+               per pass: the reduction tiling over n) and the slices of runs
+               of the canonical run reduction (its tiling over runs).
+
+Each candidate runs the same workload, timed with CUDA events on the
+launching stream; the fastest wins.  Results are cached in a JSON file keyed
+by the GPU name and the workload, so later processes reuse the choice.
 """
 import json
 import os
@@ -18,10 +26,13 @@ DEFAULT_CACHE = os.path.join(os.path.expanduser('~'), '.cache', 'pypercolate_gb3
 
 
 def _candidates(nmax, free_bytes):
-    """A compact grid: runs in flight x runs per CTA x shared-memory slot."""
+    """A compact grid: runs in flight x runs per CTA x shared-memory slot
+    (64 words hold the grids up to L = 8, 128 words up to L = 10: the
+    smallest lattices of the mix run out of shared memory)."""
     out = []
     for threads, block, smem in ((49152, 128, 0), (65536, 128, 0), (98304, 128, 0),
-                                 (65536, 64, 0), (65536, 128, 64)):
+                                 (131072, 128, 0), (65536, 64, 0), (98304, 64, 0),
+                                 (65536, 128, 64), (98304, 128, 128)):
         if 4 * nmax * threads <= 0.6 * free_bytes:
             out.append((threads, block, smem))
     return out or [(8192, 128, 0)]
@@ -75,6 +86,86 @@ def tune_mix(n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5, checkp
     if cache_path:
         os.makedirs(os.path.dirname(cache_path), exist_ok=True)
         cache[ck] = {'best': list(best[:3]), 'table': table}
+        with open(cache_path, 'w') as f:
+            json.dump(cache, f, indent=1)
+    return result
+
+
+def default_window(M, n_runs):
+    """Record-window rows nz_ensemble picks by itself: ~32 GiB of 36-byte
+    records per window, 256 .. M + 1 rows."""
+    return int(max(256, min(M + 1, 32.0 * (1 << 30) / (n_runs * 36))))
+
+
+def ensemble_candidates(M, n_runs):
+    """The library's defaults, then one launch-shape change at a time."""
+    w = default_window(M, n_runs)
+    base = {'uf_block': 128, 'm2_tile': 16, 'reduce_slices': 64 if n_runs >= 65536 else 16,
+            'window': w}
+    out = [dict(base)]
+    for key, vals in (('uf_block', (64, 32)), ('m2_tile', (8,)),
+                      ('window', (max(256, w // 2), min(M + 1, (3 * w) // 2))),
+                      ('reduce_slices', (16 if base['reduce_slices'] != 16 else 64, 256))):
+        for v in vals:
+            c = dict(base)
+            c[key] = int(v)
+            if c not in out:
+                out.append(c)
+    return out
+
+
+def tune_ensemble(kind, length, ps, n_runs, precision='fp32', micro=True, model='bond',
+                  cache_path=DEFAULT_CACHE, candidates=None, key=5, reps=2):
+    """Best launch shapes {'uf_block', 'm2_tile', 'reduce_slices', 'window'}
+    for one ensemble step of n_runs runs of this lattice and p grid, and the
+    table of all timings (the best of `reps` steps per candidate, after one
+    untimed warm-up step): {'best': {...}, 'table': [({...}, ms), ...]}."""
+    from .ensemble import Ensemble
+    torch = nat.torch_cuda()
+    ps = np.asarray(ps, dtype=np.float64)
+    spec = ('ensemble', kind, int(length), model, len(ps), float(ps.min()), float(ps.max()),
+            int(n_runs), precision, bool(micro))
+    ck = _key(spec)
+    cache = {}
+    if cache_path and os.path.exists(cache_path):
+        try:
+            cache = json.load(open(cache_path))
+        except (OSError, ValueError):
+            cache = {}
+    if ck in cache and candidates is None:
+        hit = cache[ck]
+        return {'best': hit['best'], 'table': hit['table'], 'cached': True}
+    table = []
+    stream = torch.cuda.current_stream()
+    from .ensemble import lattice_kind
+    from .hpc import GraphSpec
+    M = GraphSpec(lattice_kind(kind, model), int(length)).M
+    cands = candidates or ensemble_candidates(M, n_runs)
+    for i, cand in enumerate(cands):
+        ens = Ensemble(kind, length, ps, precision=precision, micro=micro, window=cand['window'],
+                       model=model, tuning=cand)
+        ens._ws = nat.device_empty(ens.workspace_bytes(n_runs))  # allocated outside the timing
+        if i == 0:  # the process's first steps run slower (module loading, cold TLBs)
+            ens.run(n_runs, key=key, run0=0)
+        best_ms = None
+        for rep in range(reps):
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ens.run(n_runs, key=key, run0=(rep + 1) * n_runs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best_ms = ms if best_ms is None else min(best_ms, ms)
+        table.append((dict(cand), best_ms))
+        del ens
+        torch.cuda.empty_cache()
+    best = min(table, key=lambda t: t[1])[0]
+    result = {'best': best, 'table': table, 'cached': False}
+    if cache_path:
+        os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+        cache[ck] = {'best': best, 'table': table}
         with open(cache_path, 'w') as f:
             json.dump(cache, f, indent=1)
     return result

@@ -298,6 +298,7 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
     p.w32 = nullptr;
     p.w32lo = nullptr;
     p.core_lo = p.core_len = nullptr;
+    p.m2_tile = 16;
     p.acc = out;
     p.errors = nullptr;
     launch_conv_window(p, 0, s);
@@ -415,6 +416,7 @@ constexpr double kConvF32Cutoff = 30.0;
 // mode's (+-4 standard deviations); the rest of the band holds < 1e-4 of the
 // weight and is summed in plain FP32
 constexpr double kConvCoreCutoff = 8.0;
+constexpr int32_t kMaxSlices = 256;  // slices of runs of the canonical run reduction, at most
 constexpr uint64_t kM4HighFreeNodes = 115001;  // max_s s^3 (N - s) < 2^64 for N <= 115,000
 
 // A second stream per device on which nz_ensemble runs the consumers of each
@@ -532,7 +534,8 @@ size_t ensemble_layout(Carver &c, const GraphDev &g, int32_t n_runs, int32_t P, 
     L.core_len32 = c.take<uint32_t>(P);
     L.stats = c.take<double>((size_t)n_runs * P * 7);
     L.slices = n_runs < 1024 ? 1 : (n_runs < 65536 ? 16 : 64);
-    L.part = c.take<double>((size_t)L.slices * P * 7 * 3);
+    // room for the largest tuned slice count
+    L.part = c.take<double>((size_t)kMaxSlices * P * 7 * 3);
     return c.used;
 }
 
@@ -551,7 +554,24 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
                 const double *ps, int32_t P, double cutoff, int32_t window, int32_t conv_precision,
                 void *workspace, size_t workspace_bytes, uint64_t *acc_count, double *acc_mean, double *acc_m2,
                 const NzMicroAccum *micro, void *stream) {
+    return nz_ensemble_tuned(graph, spanning, n_runs, key, run0, ps, P, cutoff, window, conv_precision, nullptr,
+                             workspace, workspace_bytes, acc_count, acc_mean, acc_m2, micro, stream);
+}
+
+int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t key, uint64_t run0,
+                      const double *ps, int32_t P, double cutoff, int32_t window, int32_t conv_precision,
+                      const NzTuning *tuning, void *workspace, size_t workspace_bytes, uint64_t *acc_count,
+                      double *acc_mean, double *acc_m2, const NzMicroAccum *micro, void *stream) {
     if (!graph || n_runs <= 0 || P <= 0 || !ps || !acc_count || !acc_mean || !acc_m2) return NZ_ERR_INVALID;
+    int32_t uf_block = 128, m2_tile = 16, slices = 0;
+    if (tuning) {
+        if (tuning->uf_block) uf_block = tuning->uf_block;
+        if (tuning->m2_tile) m2_tile = tuning->m2_tile;
+        slices = tuning->reduce_slices;
+    }
+    if ((uf_block != 32 && uf_block != 64 && uf_block != 128) || (m2_tile != 8 && m2_tile != 16) || slices < 0 ||
+        slices > kMaxSlices)
+        return NZ_ERR_INVALID;
     if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
     if (!(cutoff > 0)) cutoff = kDefaultCutoff;
     if (cutoff > kDefaultCutoff) return NZ_ERR_INVALID;  // workspace is sized for the default band
@@ -568,6 +588,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     EnsembleLayout L;
     ensemble_layout(c, g, n_runs, P, kDefaultCutoff, window, L);
     if (!workspace || !c.ok()) return NZ_ERR_WORKSPACE;
+    if (slices > 0) L.slices = slices < n_runs ? slices : n_runs;
     cudaStream_t s = as_stream(stream);
 
     {
@@ -613,6 +634,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
     cp.w32lo = L.w32lo;
     cp.core_lo = L.core_lo32;
     cp.core_len = L.core_len32;
+    cp.m2_tile = m2_tile;
     cp.acc = L.stats;
     cp.errors = L.flag + 1;  // with the union-find's corruption count
     MicroParams mp;
@@ -638,7 +660,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs, uint64_t
         up.n_begin = w0; up.n_end = w1;
         {
             ProfScope prof(NZ_PROF_UNION_FIND, s);
-            launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, 128, s);  // 64 and 256 per CTA: same time
+            launch_uf_window(up, NZ_PERM_PHILOX, spanning != 0, uf_block, s);
         }
         if (cudaEventRecord(aux.a->produced[b], s) != cudaSuccess ||
             cudaStreamWaitEvent(s2, aux.a->produced[b], 0) != cudaSuccess)

@@ -279,9 +279,10 @@ constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before 
 constexpr int kConvBatch = NZ_CONV_BATCH;  // record loads in flight per thread
 
 // Window accumulator of one canonical value.  FP64 path: an FP64 sum.  FP32
-// path: the FP32 partial sums of the row chunks are added into an FP32 TwoSum
-// (sum, compensation) pair -- as accurate as an FP64 sum of them, without
-// the FP64 pipe, which runs at 1/64 of the FP32 rate on this chip.
+// path: the FP32 partial sums of the row chunks are added into an FP32
+// (sum, compensation) pair by an error-free addition -- as accurate as an
+// FP64 sum of them, without the FP64 pipe, which runs at 1/64 of the FP32
+// rate on this chip.
 template <int PRECISION>
 struct ConvAcc {
     double v = 0.0;
@@ -291,10 +292,12 @@ struct ConvAcc {
 template <>
 struct ConvAcc<1> {
     float s = 0.0f, c = 0.0f;
+    // chunk sums and the running sum are >= 0: Fast2Sum on the operands
+    // ordered by size is exact (3 additions and a max / min, not TwoSum's 6)
     __device__ __forceinline__ void add(float x) {
-        const float t = __fadd_rn(s, x);
-        const float bp = __fsub_rn(t, s);
-        c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp)));
+        const float a = fmaxf(s, x), b = fminf(s, x);
+        const float t = __fadd_rn(a, b);
+        c = __fadd_rn(c, __fsub_rn(b, __fsub_rn(t, a)));
         s = t;
     }
     __device__ __forceinline__ double value() const { return (double)s + (double)c; }
@@ -545,19 +548,17 @@ __device__ __forceinline__ void split_u32(uint32_t q, float &qh, float &ql) {
     ql = (float)(int32_t)(q - (uint32_t)qh);
 }
 
-// 16 probabilities per CTA: each loaded record feeds twice the compensated
-// arithmetic of an 8-probability tile
-#ifndef NZ_M2_PT
-#define NZ_M2_PT 16
-#endif
-constexpr int kM2PT = NZ_M2_PT;  // probabilities per CTA of the compensated m2 kernel
 
 // grid (run tiles, tiles of kM2PT probabilities): each thread the kM2PT m2
 // values of its run.  A chunk of rows that meets the core of any of the
 // tile's probabilities runs the compensated arithmetic on all its rows
 // (branch-free, so the kM2PT accumulator chains interleave); a chunk
 // entirely in the tails runs plain FP32 products.
-template <bool NARROW>
+// kM2PT probabilities per CTA (the tuned m2_tile, 8 or 16; 16 by default:
+// each loaded record then feeds twice the compensated arithmetic of an
+// 8-probability tile, 1128 against 1218 ms per 100,000-run L = 256 step;
+// 32 measured 1285 ms)
+template <bool NARROW, int kM2PT>
 __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
     __shared__ float s_wh[kConvChunk][kM2PT], s_wl[kConvChunk][kM2PT];
     __shared__ uint32_t s_lo[kM2PT], s_len[kM2PT], s_clo[kM2PT], s_clen[kM2PT];
@@ -666,9 +667,15 @@ __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
 
 void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
-    dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kM2PT - 1) / kM2PT, 1);
-    if (p.rec.narrow) conv_m2_comp_kernel<true><<<g, kConvRuns, 0, s>>>(p);
-    else conv_m2_comp_kernel<false><<<g, kConvRuns, 0, s>>>(p);
+    const int pt = p.m2_tile == 8 ? 8 : 16;
+    dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + pt - 1) / pt, 1);
+    if (pt == 8) {
+        if (p.rec.narrow) conv_m2_comp_kernel<true, 8><<<g, kConvRuns, 0, s>>>(p);
+        else conv_m2_comp_kernel<false, 8><<<g, kConvRuns, 0, s>>>(p);
+    } else {
+        if (p.rec.narrow) conv_m2_comp_kernel<true, 16><<<g, kConvRuns, 0, s>>>(p);
+        else conv_m2_comp_kernel<false, 16><<<g, kConvRuns, 0, s>>>(p);
+    }
 }
 
 bool conv_grid_fits(int32_t n_runs, int32_t P) {

@@ -44,6 +44,16 @@ constexpr int kTcP = 32;      // N: probabilities per CTA
 constexpr int kTcK = NZ_TC_K;  // rows per chunk (16 or 32): kTcK / 8 MMAs of K = 8
 static_assert(kTcK == 16 || kTcK == 32, "chunk of 16 or 32 rows");
 constexpr uint32_t kTcCols = 2 * kTcP;                // TMEM columns: two FP32 accumulators
+// chunks accumulated in TMEM (FP32) before the threads drain them into their
+// (sum, compensation) pairs.  The tensor cores' FP32 accumulation rounds
+// toward zero: over 8 chunks (128 rows, 48 accumulation steps per drain)
+// every curve came out ~2e-6 relative low (the strength 1.7e-6 absolute at
+// L = 256), over one chunk (6 steps) within 2.3e-7 -- so each chunk is
+// drained
+#ifndef NZ_TC_DRAIN
+#define NZ_TC_DRAIN 1
+#endif
+constexpr uint32_t kTcDrain = NZ_TC_DRAIN;
 constexpr uint32_t kCoreBytes = 128;                  // core matrix: 8 rows x 16 bytes
 constexpr uint32_t kSbo = (kTcK / 4) * kCoreBytes;    // between 8-row groups
 
@@ -93,13 +103,14 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
     lo = to_tf32(__fsub_rn(x, hi));
 }
 
-// TwoSum (Knuth): s + x = t + err exactly; err collected in c
+// s + x = t + err exactly, err collected in c.  The chunk sums and the
+// running sum are >= 0, so Dekker's Fast2Sum on the operands ordered by size
+// (max / min) is exact: 3 additions instead of Knuth's TwoSum's 6.
 __device__ __forceinline__ void two_sum_add(float &s, float &c, float x) {
-    const float t = __fadd_rn(s, x);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    const float a = fmaxf(s, x), b = fminf(s, x);
+    const float t = __fadd_rn(a, b);
+    c = __fadd_rn(c, __fsub_rn(b, __fsub_rn(t, a)));
     s = t;
-    c = __fadd_rn(c, err);
 }
 
 // Raw record words of one chunk's rows: the plane statistic S reads (m4_lo
@@ -236,13 +247,16 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
         if (__syncthreads_or(bad)) break;  // a wait below gave up
         if (t == 0) {
             tc_fence_after();
-            const uint32_t d = tmem + (uint32_t)(st * kTcP);
+            // accumulator of this chunk's period of kTcDrain chunks; a
+            // period's first chunk overwrites it
+            const uint32_t d = tmem + (uint32_t)(((ch / kTcDrain) & 1) * kTcP);
+            const bool fresh = ch % kTcDrain == 0;
             const uint32_t ah = smem_u32(sh.a[st][0]), al = smem_u32(sh.a[st][1]);
             const uint32_t bh = smem_u32(sh.b[st][0]), bl = smem_u32(sh.b[st][1]);
 #pragma unroll
             for (int ks = 0; ks < kTcK / 8; ++ks) {
                 const uint32_t o = (uint32_t)ks * 2 * kCoreBytes;  // K = 8: two core matrices
-                mma_tf32(d, smem_desc(ah + o), smem_desc(bh + o), ks > 0 ? 1u : 0u);
+                mma_tf32(d, smem_desc(ah + o), smem_desc(bh + o), (ks > 0 || !fresh) ? 1u : 0u);
                 mma_tf32(d, smem_desc(ah + o), smem_desc(bl + o), 1u);
                 if (S != 0) mma_tf32(d, smem_desc(al + o), smem_desc(bh + o), 1u);  // spanning: lo = 0
             }
@@ -250,11 +264,14 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
         }
         if (ch > 0) {
             const uint32_t pc = ch - 1;
-            bad = !mbar_wait(smem_u32(&sh.mbar[pc & 1]), (pc >> 1) & 1);
-            if (!bad) {
+            // chunk ch - 1's MMAs done: its shared-memory stage is free, and
+            // if it closed a period, that period's accumulator is complete
+            // (warp-uniform: tcgen05.ld is executed by the whole warp)
+            bad = !__all_sync(0xffffffffu, mbar_wait(smem_u32(&sh.mbar[pc & 1]), (pc >> 1) & 1));
+            if (!bad && pc % kTcDrain == kTcDrain - 1) {
                 tc_fence_after();
                 float v[kTcP];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((pc & 1) * kTcP), v);
+                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(((pc / kTcDrain) & 1) * kTcP), v);
 #pragma unroll
                 for (int j = 0; j < kTcP; ++j) two_sum_add(acc_s[j], acc_c[j], v[j]);
             }
@@ -264,14 +281,16 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     const uint32_t issued = ch;
     if (issued > 0) {
         const uint32_t pc = issued - 1;
-        const bool ok = mbar_wait(smem_u32(&sh.mbar[pc & 1]), (pc >> 1) & 1);
-        if (ok && !bad) {
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&sh.mbar[pc & 1]), (pc >> 1) & 1));
+        // the last period: the loop drains a period when it waits for the
+        // chunk after it, which the last one does not have
+        if (ok && !__any_sync(0xffffffffu, bad)) {
             tc_fence_after();
             float v[kTcP];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((pc & 1) * kTcP), v);
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(((pc / kTcDrain) & 1) * kTcP), v);
 #pragma unroll
             for (int j = 0; j < kTcP; ++j) two_sum_add(acc_s[j], acc_c[j], v[j]);
-        } else {
+        } else if (!ok) {
             bad = true;
         }
     }

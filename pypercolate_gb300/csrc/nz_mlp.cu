@@ -78,11 +78,18 @@ __device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uin
 __global__ void __launch_bounds__(kGM) mlp_gemm_kernel(int M, int N, int K, const float *A, int sam, int sak,
                                                        const float *Bf, const __nv_bfloat16 *Bh, int sbk, int sbn,
                                                        const float *bias, int epilogue, float *Z, float *C,
-                                                       int ldc, int accumulate, int ntile) {
+                                                       int ldc, int accumulate, int ntile, int k_split) {
     extern __shared__ __align__(1024) uint8_t gemm_smem[];
     GemmSmem &sh = *reinterpret_cast<GemmSmem *>(gemm_smem);
     const int t = threadIdx.x, warp = t >> 5;
     const int m0 = blockIdx.y * kGM, n0 = blockIdx.x * ntile;
+    // split-K: this CTA's K range [kb, kb + k_split); its tile goes to slice
+    // blockIdx.z of C (M x ldc floats per slice)
+    const int kb = blockIdx.z * k_split;
+    if (gridDim.z > 1) {
+        K = min(K - kb, k_split);
+        C += (size_t)blockIdx.z * M * ldc;
+    }
     const uint32_t cols = ntile <= 32 ? 32u : (ntile <= 64 ? 64u : 128u);  // TMEM: power of two >= 32
     if (warp == 0) tc::tmem_alloc(tc::smem_u32(&sh.tmem), cols);
     if (t == 0) {
@@ -105,7 +112,7 @@ __global__ void __launch_bounds__(kGM) mlp_gemm_kernel(int M, int N, int K, cons
             const int r = a_kfast ? i / kGK : i % kGM;
             const int k = a_kfast ? i % kGK : i / kGM;
             const int gm = m0 + r, gk = k0 + k;
-            const float v = (gm < M && gk < K) ? A[(size_t)gm * sam + (size_t)gk * sak] : 0.0f;
+            const float v = (gm < M && gk < K) ? A[(size_t)gm * sam + (size_t)(kb + gk) * sak] : 0.0f;
             sa[kmajor_idx(r, k)] = __float2bfloat16_rn(v);
         }
         for (int i = t; i < ntile * kGK; i += kGM) {
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(kGM) mlp_gemm_kernel(int M, int N, int K, cons
             const int gn = n0 + r, gk = k0 + k;
             __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
             if (gn < N && gk < K) {
-                const size_t idx = (size_t)gk * sbk + (size_t)gn * sbn;
+                const size_t idx = (size_t)(kb + gk) * sbk + (size_t)gn * sbn;
                 v = Bh ? Bh[idx] : __float2bfloat16_rn(Bf[idx]);
             }
             sb[kmajor_idx(r, k)] = v;
@@ -181,17 +188,45 @@ __global__ void __launch_bounds__(kGM) mlp_gemm_kernel(int M, int N, int K, cons
     }
 }
 
+// slices[z][m][n] summed over z in order into C (deterministic split-K)
+__global__ void splitk_sum_kernel(const float *slices, int splits, int M, int N, int ldc, float *C) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i / N), n = (int)(i % N);
+        float acc = 0.0f;
+        for (int z = 0; z < splits; ++z) acc += slices[(size_t)z * M * ldc + (size_t)m * ldc + n];
+        C[(size_t)m * ldc + n] = acc;
+    }
+}
+
+// C = A B (+ bias, epilogue).  With `partial` (room for `splits` x M x ldc
+// floats) and splits > 1, K is split over that many CTAs per tile, for GEMMs
+// with few output tiles and a long K (the weight gradients: K = batch); the
+// slices are then summed in order (no bias, no epilogue, C overwritten).
 static void gemm(int M, int N, int K, const float *A, int sam, int sak, const float *Bf, const __nv_bfloat16 *Bh,
                  int sbk, int sbn, const float *bias, int epilogue, float *Z, float *C, int ldc, int accumulate,
-                 cudaStream_t s) {
+                 cudaStream_t s, float *partial = nullptr, int splits = 1) {
     if (M <= 0 || N <= 0) return;
     const int ntile = N >= kGN ? kGN : ((N + 15) / 16) * 16;
+    int k_split = K;
+    if (partial && splits > 1) {
+        k_split = ((K + splits - 1) / splits + kGK - 1) / kGK * kGK;
+        splits = (K + k_split - 1) / k_split;
+    }
+    if (splits < 2) { partial = nullptr; splits = 1; k_split = K; }
     // above 48 KB of dynamic shared memory the launch needs the attribute,
     // which belongs to the function in the current device's context
     cudaFuncSetAttribute(mlp_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GemmSmem));
-    dim3 grid((N + ntile - 1) / ntile, (M + kGM - 1) / kGM);
-    mlp_gemm_kernel<<<grid, kGM, sizeof(GemmSmem), s>>>(M, N, K, A, sam, sak, Bf, Bh, sbk, sbn, bias, epilogue, Z,
-                                                         C, ldc, accumulate, ntile);
+    dim3 grid((N + ntile - 1) / ntile, (M + kGM - 1) / kGM, splits);
+    mlp_gemm_kernel<<<grid, kGM, sizeof(GemmSmem), s>>>(M, N, K, A, sam, sak, Bf, Bh, sbk, sbn,
+                                                         partial ? nullptr : bias, partial ? 0 : epilogue, Z,
+                                                         partial ? partial : C, ldc, partial ? 0 : accumulate,
+                                                         ntile, k_split);
+    if (partial) {
+        const int64_t total = (int64_t)M * N;
+        const int blocks = (int)((total + 255) / 256 > 1024 ? 1024 : (total + 255) / 256);
+        splitk_sum_kernel<<<blocks, 256, 0, s>>>(partial, splits, M, N, ldc, C);
+    }
 }
 
 __global__ void to_bf16_kernel(const float *a, __nv_bfloat16 *b, int64_t n) {
@@ -352,8 +387,12 @@ int nz_mlp_backward(const int32_t *widths, int32_t n_layers, int32_t batch, cons
     for (int l = n_layers - 1; l >= 0; --l) {
         const int K = widths[l], N = widths[l + 1];
         const float *A = l == 0 ? x : h + act_off[l - 1];
-        // dW[K][N] = A^T dZ  (reduction over the batch)
-        gemm(K, N, batch, A, 1, K, dZ, nullptr, N, 1, nullptr, 0, nullptr, grads + wo[l], N, 0, s);
+        // dW[K][N] = A^T dZ  (reduction over the batch), split over the batch
+        // into slices held in the dA half of the scratch (free until the dA
+        // GEMM below): splits * K * N <= batch * wmax floats
+        const int64_t room = (int64_t)batch * wmax / ((int64_t)K * N);
+        const int splits = (int)(room < 32 ? room : 32);
+        gemm(K, N, batch, A, 1, K, dZ, nullptr, N, 1, nullptr, 0, nullptr, grads + wo[l], N, 0, s, dA, splits);
         bias_grad_kernel<<<N, 256, 0, s>>>(dZ, batch, N, grads + bo[l]);
         if (l == 0) break;
         // dA[batch][K] = dZ W^T  (W[K][N]: B(k=n, n=k) = W[k][n] -> sbk = 1, sbn = N)

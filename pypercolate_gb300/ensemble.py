@@ -54,10 +54,12 @@ class Ensemble:
               sums per 32-row chunk added into TwoSum pairs) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
     window    rows per union-find launch (0: sized to ~32 GiB of records per window)
+    tuning    launch shapes {'uf_block', 'm2_tile', 'reduce_slices'} (autotune.tune_ensemble
+              picks them; None: the library's defaults)
     """
 
     def __init__(self, kind='grid', length=16, ps=None, spanning=True, precision='fp32',
-                 micro=True, window=0, cutoff=80.0, model='bond', wrap='either'):
+                 micro=True, window=0, cutoff=80.0, model='bond', wrap='either', tuning=None):
         torch = nat.torch_cuda()
         self.kind = kind
         self.model = model
@@ -72,6 +74,7 @@ class Ensemble:
         self.precision = PRECISIONS.index(precision)
         self.window = int(window)
         self.cutoff = float(cutoff)
+        self.tuning = dict(tuning) if tuning else None
         self.d_ps = torch.from_numpy(self.ps.copy()).to('cuda')
         self.count = torch.zeros(1, dtype=torch.int64, device='cuda')
         self.mean = torch.zeros(self.P * 7, dtype=torch.float64, device='cuda')
@@ -112,12 +115,16 @@ class Ensemble:
             self._ws = None
             self._ws = nat.device_empty(need)
         micro = self._micro_struct()
-        st = lib.nz_ensemble(g, int(self.spanning), n_runs, int(key), int(run0),
-                             nat.ptr(self.d_ps), self.P, self.cutoff, self.window,
-                             self.precision, nat.ptr(self._ws), self._ws.numel(),
-                             nat.ptr(self.count), nat.ptr(self.mean), nat.ptr(self.m2),
-                             micro, nat.stream_handle(stream))
-        nat.check(st, 'nz_ensemble')
+        tune = None
+        if self.tuning:
+            tune = nat.NzTuning(int(self.tuning.get('uf_block', 0)), int(self.tuning.get('m2_tile', 0)),
+                                int(self.tuning.get('reduce_slices', 0)))
+        st = lib.nz_ensemble_tuned(g, int(self.spanning), n_runs, int(key), int(run0),
+                                   nat.ptr(self.d_ps), self.P, self.cutoff, self.window,
+                                   self.precision, tune, nat.ptr(self._ws), self._ws.numel(),
+                                   nat.ptr(self.count), nat.ptr(self.mean), nat.ptr(self.m2),
+                                   micro, nat.stream_handle(stream))
+        nat.check(st, 'nz_ensemble_tuned')
         self.ledger.append((int(key), int(run0), n_runs))
         self._last_runs = n_runs
         return self

@@ -105,3 +105,24 @@ def test_surrogate_pipeline_small(gpu):
     err_placed = np.max(np.abs(np.interp(dense, placed, np.interp(placed, dense, truth[:, 0]))
                                - truth[:, 0]))
     assert err_placed < err_uni
+
+
+def test_pick_next_length_prefers_the_lattice_the_surrogate_knows_least(gpu):
+    """Trained on square lattices L in {8..32}, the surrogate is judged by
+    cheap pilot ensembles at three candidate lengths; the one far outside the
+    training range (L = 128) disagrees most with it, in Monte Carlo standard
+    errors, and is the one to simulate next."""
+    from pypercolate_gb300 import surrogate as S
+    ps = np.linspace(0.0, 1.0, 401)
+    X, Y = [], []
+    for L in (8, 12, 16, 20, 24, 28, 32):
+        y, _ = S.ensemble_targets('grid', L, ps, 1500, key=L)
+        X.append(S.features(ps, L, 'grid'))
+        Y.append(y)
+    model = S.MLP(seed=1)
+    model.fit(np.concatenate(X), np.concatenate(Y), steps=1500, batch=4096, lr=1e-3)
+    cands = [16, 24, 128]
+    choice, scores = S.pick_next_length(model, cands, 'grid', pilot_runs=400)
+    assert len(scores) == 3 and all(np.isfinite(scores))
+    assert choice == 128
+    assert scores[2] > max(scores[0], scores[1])

@@ -625,7 +625,9 @@ def main():
                'launch': {'threads': threads, 'block': block, 'smem_words': smem},
                'autotune': [list(t) for t in tuned['table']], 'cuda_graph': True,
                'workload': '2D L log-uniform [8,512] + chains l log-uniform [1024,65536], '
-                           '50/50, 256 checkpoints, exact per-lattice reductions'}
+                           '50/50, 256 checkpoints, exact per-lattice reductions; union-find '
+                           'and microcanonical checkpoint reductions only (no canonical '
+                           'convolution), in both this leg and its plain leg'}
         del me
         torch.cuda.empty_cache()
         if args.plain_mix:

@@ -175,8 +175,9 @@ def parse():
                     help='timed runs re-run in FP64 for the per-curve error (0: skip)')
     ap.add_argument('--mix-runs', type=int, default=1000000,
                     help='runs of the batched uneven workload (0: skip)')
-    ap.add_argument('--study', default=None, choices=[None, 'precision', 'surrogate'],
-                    help='precision: FP32 vs FP64 canonical curves at L=1024 (separate line)')
+    ap.add_argument('--study', default=None, choices=[None, 'precision', 'surrogate', 'mlp'],
+                    help='precision: FP32 vs FP64 canonical curves at L=1024; surrogate: train '
+                         'and judge the MLP surrogate; mlp: MLP training throughput (separate lines)')
     ap.add_argument('--lattice', default='grid', choices=['grid', 'torus'],
                     help='main leg lattice: spanning_2d_grid or the periodic square lattice '
                          '(wrapping in either direction); for profiling the extensions')
@@ -459,6 +460,30 @@ def surrogate_study(args):
     return 0
 
 
+def mlp_study(args):
+    """Training throughput of the MLP surrogate's kernels (tcgen05 BF16
+    GEMMs, GELU, loss, Adam): `args.steps` Adam steps of batch 4096 on
+    20,000 synthetic rows after `args.warmup` warm-up steps."""
+    import torch
+    from pypercolate_gb300.surrogate import MLP, WIDTHS
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(0)
+    X = rng.uniform(0, 1, size=(20000, WIDTHS[0])).astype(np.float32)
+    Y = np.column_stack([np.tanh(8 * (X[:, 0] - 0.5)), X[:, 1] ** 2, np.sin(3 * X[:, 2])])
+    model = MLP(seed=2)
+    model.fit(X, Y, steps=max(1, args.warmup), batch=4096)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    trace = model.fit(X, Y, steps=args.steps, batch=4096, lr=1e-3, log_every=max(1, args.steps // 2))
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    print(json.dumps({'study': 'MLP training throughput', 'widths': list(WIDTHS), 'batch': 4096,
+                      'steps': args.steps, 'samples_per_s': args.steps * 4096 / dt,
+                      'ms_per_step': dt / args.steps * 1e3, 'final_loss': trace[-1][1],
+                      'gemm': 'tcgen05.mma kind::f16 (BF16 operands, FP32 TMEM accumulator)'}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
@@ -467,6 +492,8 @@ def main():
         return precision_study(args)
     if args.study == 'surrogate':
         return surrogate_study(args)
+    if args.study == 'mlp':
+        return mlp_study(args)
     import torch
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
@@ -483,13 +510,13 @@ def main():
     ps = np.linspace(0.0, 1.0, args.P)
     # launch shapes from the autotuner, timed on this workload (before the
     # main ensemble holds its workspace)
-    tuned = None
+    ens_tuned = None
     tuning, window = None, args.window
     if args.tune:
         from pypercolate_gb300.autotune import tune_ensemble
-        tuned = tune_ensemble(args.lattice, L, ps, R, precision=args.precision,
-                              micro=not args.no_micro, model=args.model, cache_path=None)
-        tuning = tuned['best']
+        ens_tuned = tune_ensemble(args.lattice, L, ps, R, precision=args.precision,
+                                  micro=not args.no_micro, model=args.model, cache_path=None)
+        tuning = ens_tuned['best']
         window = window or tuning['window']
     ens = Ensemble(args.lattice, L, ps, precision=args.precision, micro=not args.no_micro,
                    window=window, model=args.model, tuning=tuning)
@@ -691,10 +718,11 @@ def main():
                             'plain': plain['union_find_only'] if plain else None},
         'curve_err_vs_fp64': curve_err,
         'clocks': clocks,
-        'autotune': ({'best': tuned['best'],
-                      'table': [[c, ms] for c, ms in tuned['table']],
-                      'candidates_ms': 'one ensemble step of the workload per candidate'}
-                     if tuned else None),
+        'autotune': ({'best': ens_tuned['best'],
+                      'table': [[c, ms] for c, ms in ens_tuned['table']],
+                      'candidates_ms': 'one ensemble step of the workload per candidate '
+                                       '(best of two after a warm-up step)'}
+                     if ens_tuned else None),
         'gpu_launches': gpu_launches,
         'merged_runs': merged_runs,
         'union_find_errors': uf_errors,

@@ -43,15 +43,20 @@ constexpr int kTcP = 32;      // N: probabilities per CTA
 #endif
 constexpr int kTcK = NZ_TC_K;  // rows per chunk (16 or 32): kTcK / 8 MMAs of K = 8
 static_assert(kTcK == 16 || kTcK == 32, "chunk of 16 or 32 rows");
-constexpr uint32_t kTcCols = 2 * kTcP;                // TMEM columns: two FP32 accumulators
+// TMEM columns: for each of two periods in flight, a main accumulator (the
+// hi x hi products) and a correction accumulator (hi x lo + lo x hi)
+constexpr uint32_t kTcCols = 4 * kTcP;
 // chunks accumulated in TMEM (FP32) before the threads drain them into their
 // (sum, compensation) pairs.  The tensor cores' FP32 accumulation rounds
-// toward zero: over 8 chunks (128 rows, 48 accumulation steps per drain)
-// every curve came out ~2e-6 relative low (the strength 1.7e-6 absolute at
-// L = 256), over one chunk (6 steps) within 2.3e-7 -- so each chunk is
-// drained
+// toward zero, so its error grows with the accumulation steps between
+// drains: with all three products in one accumulator, 8 chunks (48 steps)
+// left every curve ~2e-6 relative low (the strength 1.7e-6 absolute at
+// L = 256), one chunk (6 steps) within 2.3e-7.  With the corrections (~2^-11
+// of the main terms) in their own accumulator, the main one takes 2 steps
+// per chunk: 4 chunks are 8 steps, and a drain every 4 chunks costs the
+// threads a quarter of a drain every chunk
 #ifndef NZ_TC_DRAIN
-#define NZ_TC_DRAIN 1
+#define NZ_TC_DRAIN 4
 #endif
 constexpr uint32_t kTcDrain = NZ_TC_DRAIN;
 constexpr uint32_t kCoreBytes = 128;                  // core matrix: 8 rows x 16 bytes
@@ -192,6 +197,19 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
     float acc_s[kTcP], acc_c[kTcP];
 #pragma unroll
     for (int j = 0; j < kTcP; ++j) acc_s[j] = acc_c[j] = 0.0f;
+    // a period's sums of this thread's run (TMEM lane t): the main terms
+    // into the (sum, compensation) pairs, the corrections into the
+    // compensation
+    auto drain = [&](uint32_t q) {
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + q * 2 * kTcP;
+        float v[kTcP];
+        tmem_ld32(lane_base, v);
+#pragma unroll
+        for (int j = 0; j < kTcP; ++j) two_sum_add(acc_s[j], acc_c[j], v[j]);
+        tmem_ld32(lane_base + kTcP, v);
+#pragma unroll
+        for (int j = 0; j < kTcP; ++j) acc_c[j] = __fadd_rn(acc_c[j], v[j]);
+    };
     raw_word<S> raw[kTcK];
     uint64_t raw_hi[S == 6 ? kTcK : 1];
     load_chunk<S>(p.rec, base, stride, 0, last, raw, raw_hi);
@@ -247,18 +265,19 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
         if (__syncthreads_or(bad)) break;  // a wait below gave up
         if (t == 0) {
             tc_fence_after();
-            // accumulator of this chunk's period of kTcDrain chunks; a
-            // period's first chunk overwrites it
-            const uint32_t d = tmem + (uint32_t)(((ch / kTcDrain) & 1) * kTcP);
+            // accumulators of this chunk's period of kTcDrain chunks; a
+            // period's first chunk overwrites them
+            const uint32_t d = tmem + (uint32_t)(((ch / kTcDrain) & 1) * 2 * kTcP), dc = d + kTcP;
             const bool fresh = ch % kTcDrain == 0;
             const uint32_t ah = smem_u32(sh.a[st][0]), al = smem_u32(sh.a[st][1]);
             const uint32_t bh = smem_u32(sh.b[st][0]), bl = smem_u32(sh.b[st][1]);
 #pragma unroll
             for (int ks = 0; ks < kTcK / 8; ++ks) {
                 const uint32_t o = (uint32_t)ks * 2 * kCoreBytes;  // K = 8: two core matrices
-                mma_tf32(d, smem_desc(ah + o), smem_desc(bh + o), (ks > 0 || !fresh) ? 1u : 0u);
-                mma_tf32(d, smem_desc(ah + o), smem_desc(bl + o), 1u);
-                if (S != 0) mma_tf32(d, smem_desc(al + o), smem_desc(bh + o), 1u);  // spanning: lo = 0
+                const uint32_t acc = (ks > 0 || !fresh) ? 1u : 0u;
+                mma_tf32(d, smem_desc(ah + o), smem_desc(bh + o), acc);
+                mma_tf32(dc, smem_desc(ah + o), smem_desc(bl + o), acc);
+                if (S != 0) mma_tf32(dc, smem_desc(al + o), smem_desc(bh + o), 1u);  // spanning: lo = 0
             }
             mma_commit(smem_u32(&sh.mbar[st]));
         }
@@ -270,10 +289,7 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
             bad = !__all_sync(0xffffffffu, mbar_wait(smem_u32(&sh.mbar[pc & 1]), (pc >> 1) & 1));
             if (!bad && pc % kTcDrain == kTcDrain - 1) {
                 tc_fence_after();
-                float v[kTcP];
-                tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(((pc / kTcDrain) & 1) * kTcP), v);
-#pragma unroll
-                for (int j = 0; j < kTcP; ++j) two_sum_add(acc_s[j], acc_c[j], v[j]);
+                drain((pc / kTcDrain) & 1);
             }
         }
     }
@@ -286,10 +302,7 @@ __device__ __forceinline__ void conv_tc_tile(const ConvParams &p, TcShared &sh, 
         // chunk after it, which the last one does not have
         if (ok && !__any_sync(0xffffffffu, bad)) {
             tc_fence_after();
-            float v[kTcP];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(((pc / kTcDrain) & 1) * kTcP), v);
-#pragma unroll
-            for (int j = 0; j < kTcP; ++j) two_sum_add(acc_s[j], acc_c[j], v[j]);
+            drain((pc / kTcDrain) & 1);
         } else if (!ok) {
             bad = true;
         }

@@ -416,19 +416,19 @@ def surrogate_study(args):
         grid = S.training_grid(kind, L, P)
         y, _ = S.ensemble_targets(kind, L, grid, runs, key=L)
         X.append(S.features(grid, L, kind))
-        Y.append(y)
+        Y.append(S.train_targets(y))
     X, Y = np.concatenate(X), np.concatenate(Y)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     model = S.MLP(seed=0)
-    steps, batch = 12000, 4096
+    steps, batch = 30000, 4096
     t0 = time.perf_counter()
     trace = model.fit(X, Y, steps=steps, batch=batch, lr=1e-3, log_every=1000, decay=0.05)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     dense = np.linspace(0.0, 1.0, 2001)
     truth, se = S.ensemble_targets('grid', 384, dense, 8000, key=384384)
-    pred = model.predict(S.features(dense, 384, 'grid'))
+    pred = S.curves(model.predict(S.features(dense, 384, 'grid')))
     acc = {}
     cheap, cheap_se = S.ensemble_targets('grid', 384, dense, 400, key=384400)
     for j, name in enumerate(S.OUTPUTS):

@@ -6,9 +6,11 @@ asinh((p - p_c) L^(1/nu)) derived from them (p_c = 1/2, nu = 4/3 for bond
 percolation on the square lattice; p_c = 1, nu = 1 for the chain), on which
 the curves of different L collapse -- to (spanning probability, percolation
 strength, log-susceptibility), where susceptibility = m2 / N (the mean size
-of the non-largest clusters, sum' s^2 / N).  It is trained with the
-library's own BF16/FP32 forward, backward and Adam kernels (libnzgb300
-``nz_mlp_*``) on ensembles that this package's GPU path generates.
+of the non-largest clusters, sum' s^2 / N); the strength is learned as its
+logarithm (``train_targets``, ``curves``).  It is trained with the library's
+own forward, backward and Adam kernels (libnzgb300 ``nz_mlp_*``: tcgen05
+GEMMs with BF16 operands and FP32 accumulation) on ensembles that this
+package's GPU path generates.
 
 The Monte Carlo estimate stays the judge and the fallback: a surrogate value
 is accepted only where it lies within ``accept_sigma`` Monte Carlo standard
@@ -80,6 +82,27 @@ def ensemble_targets(kind, L, ps, runs, key=11, run0=0, precision='fp32'):
     y = np.column_stack([span, strength, log_chi])
     s = np.column_stack([span_se, strength_se, log_chi_se])
     return y, s
+
+
+STRENGTH_FLOOR = 1e-12
+
+
+def train_targets(y):
+    """The curves as the network learns them: spanning probability as is,
+    log strength and log susceptibility.  Below the threshold the strength
+    is ~log(N)/N and its Monte Carlo error ~1e-6: in log units the network's
+    error is relative, so it can come within the judge's error bars there."""
+    out = np.array(y, dtype=np.float64, copy=True)
+    out[:, 1] = np.log(np.maximum(out[:, 1], STRENGTH_FLOOR))
+    return out
+
+
+def curves(pred):
+    """Network outputs back to (spanning probability, strength, log
+    susceptibility)."""
+    out = np.array(pred, dtype=np.float64, copy=True)
+    out[:, 1] = np.exp(out[:, 1])
+    return out
 
 
 class MLP:
@@ -223,7 +246,7 @@ def place_p_grid(model, L, kind, k, lo=0.0, hi=1.0, dense=4001, floor=0.05):
     """k probabilities placed where the surrogate's spanning curve changes
     fastest: quantiles of the density |dPi/dp| + floor * mean|dPi/dp|."""
     p = np.linspace(lo, hi, dense)
-    pi = model.predict(features(p, L, kind))[:, 0]
+    pi = curves(model.predict(features(p, L, kind)))[:, 0]
     d = np.abs(np.gradient(pi, p))
     d = d + floor * d.mean() + 1e-12
     cdf = np.concatenate([[0.0], np.cumsum(0.5 * (d[1:] + d[:-1]) * np.diff(p))])
@@ -240,7 +263,7 @@ def pick_next_length(model, candidates, kind, pilot_runs=200, ps=None, key=99):
     scores = []
     for L in candidates:
         y, s = ensemble_targets(kind, L, ps, pilot_runs, key=key)
-        pred = model.predict(features(ps, L, kind))
+        pred = curves(model.predict(features(ps, L, kind)))
         z = np.abs(pred[:, 0] - y[:, 0]) / np.maximum(s[:, 0], 1e-6)
         scores.append(float(np.mean(z)))
     return candidates[int(np.argmax(scores))], scores

@@ -83,12 +83,12 @@ def test_surrogate_pipeline_small(gpu):
     for L in (8, 12, 16, 20, 24, 32, 40, 48):
         y, _ = S.ensemble_targets('grid', L, ps, 1500, key=L)
         X.append(S.features(ps, L, 'grid'))
-        Y.append(y)
+        Y.append(S.train_targets(y))
     model = S.MLP(seed=0)
     model.fit(np.concatenate(X), np.concatenate(Y), steps=1500, batch=4096, lr=1e-3)
     dense = np.linspace(0.0, 1.0, 1001)
     truth, truth_se = S.ensemble_targets('grid', 28, dense, 4000, key=2828)
-    pred = model.predict(S.features(dense, 28, 'grid'))
+    pred = S.curves(model.predict(S.features(dense, 28, 'grid')))
     values, ok = S.judged(pred[:, 0], truth[:, 0], truth_se[:, 0])
     # the Monte Carlo estimate is the fallback wherever the surrogate is rejected
     assert np.array_equal(values[~ok], truth[~ok, 0])
@@ -118,7 +118,7 @@ def test_pick_next_length_prefers_the_lattice_the_surrogate_knows_least(gpu):
     for L in (8, 12, 16, 20, 24, 28, 32):
         y, _ = S.ensemble_targets('grid', L, ps, 1500, key=L)
         X.append(S.features(ps, L, 'grid'))
-        Y.append(y)
+        Y.append(S.train_targets(y))
     model = S.MLP(seed=1)
     model.fit(np.concatenate(X), np.concatenate(Y), steps=1500, batch=4096, lr=1e-3)
     cands = [16, 24, 128]

@@ -662,7 +662,9 @@ def main():
             mix['batched_vs_plain'] = mix['value'] / mix['plain']['value']
 
     # end to end through the public API: inputs (p-grid) from pinned host
-    # memory, results (finalized canonical averages) read back every step
+    # memory, results read back every step -- the finalized canonical
+    # averages and, with the fused micro reductions on, the microcanonical
+    # averages of every n (means and confidence bounds, 21 values per n)
     h_ps = torch.from_numpy(ps.copy()).pin_memory()
     h2d = h_ps.numel() * 8
     d2h = 0
@@ -676,6 +678,9 @@ def main():
         e.run(R, key=KEY, run0=run_base + 10 ** 8 + k * R)
         fin = e.finalized(0.05)
         d2h = fin.nbytes + e.canonical_averages().nbytes
+        if e.micro is not None:
+            mic = e.microcanonical_averages(0.05)
+            d2h += sum(v.nbytes for v in mic.values() if isinstance(v, np.ndarray))
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     e2e_value = R * M * world / e2e_s

@@ -351,13 +351,19 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
  * package's autotune.tune_ensemble) rather than fixed; a field of 0 takes the
  * default.  uf_block: runs per CTA of the union-find (32, 64 or 128; 128);
  * m2_tile: probabilities per CTA of the compensated m2 convolution (8 or 16;
- * 16); reduce_slices: slices of runs of the canonical run reduction (1 ..
- * 256; 1, 16 or 64 by run count).  The record window is nz_ensemble's
- * `window`.  No counterpart in the reference (its runs are Python calls). */
+ * 8); reduce_slices: slices of runs of the canonical run reduction (1 ..
+ * 256; 1, 16 or 64 by run count); conv_tile: probabilities per CTA of the
+ * FP32 convolution kernels of the other statistics (8 or 16; 8); taper: 1 =
+ * the first and the last record window a quarter window long (the first
+ * window's union-find and the last window's reductions run alone), 0 = all
+ * windows full (0).  The record window is nz_ensemble's `window`.  No
+ * counterpart in the reference (its runs are Python calls). */
 typedef struct NzTuning {
     int32_t uf_block;
     int32_t m2_tile;
     int32_t reduce_slices;
+    int32_t conv_tile;
+    int32_t taper;
 } NzTuning;
 /* nz_ensemble with explicit launch shapes (tuning may be NULL: defaults);
  * results do not depend on them beyond the order of FP64 additions in the

@@ -60,7 +60,8 @@ class NzMicroAccum(ctypes.Structure):
 
 class NzTuning(ctypes.Structure):
     _fields_ = [('uf_block', ctypes.c_int32), ('m2_tile', ctypes.c_int32),
-                ('reduce_slices', ctypes.c_int32)]
+                ('reduce_slices', ctypes.c_int32), ('conv_tile', ctypes.c_int32),
+                ('taper', ctypes.c_int32)]
 
 
 class NzMixSpec(ctypes.Structure):

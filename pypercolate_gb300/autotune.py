@@ -5,8 +5,9 @@ tune_mix       batched uneven ensembles (``nz_mix``): persistent threads
                shared-memory node slot per thread (placement: small lattices
                in shared memory, the rest in HBM / L2).
 tune_ensemble  one lattice per ensemble (``nz_ensemble_tuned``): runs per
-               CTA of the union-find, the probability tile of the compensated
-               m2 convolution, the record window (rows reduced and convolved
+               CTA of the union-find, the probability tiles of the compensated
+               m2 convolution and of the other statistics' convolution, the
+               record window (rows reduced and convolved
                per pass: the reduction tiling over n) and the slices of runs
                of the canonical run reduction (its tiling over runs).
 
@@ -100,10 +101,10 @@ def default_window(M, n_runs):
 def ensemble_candidates(M, n_runs):
     """The library's defaults, then one launch-shape change at a time."""
     w = default_window(M, n_runs)
-    base = {'uf_block': 128, 'm2_tile': 16, 'reduce_slices': 64 if n_runs >= 65536 else 16,
-            'window': w}
+    base = {'uf_block': 128, 'm2_tile': 8, 'conv_tile': 8, 'taper': 0,
+            'reduce_slices': 64 if n_runs >= 65536 else 16, 'window': w}
     out = [dict(base)]
-    for key, vals in (('uf_block', (64, 32)), ('m2_tile', (8,)),
+    for key, vals in (('uf_block', (64, 32)), ('m2_tile', (16,)), ('conv_tile', (16,)), ('taper', (1,)),
                       ('window', (max(256, w // 2), min(M + 1, (3 * w) // 2))),
                       ('reduce_slices', (16 if base['reduce_slices'] != 16 else 64, 256))):
         for v in vals:
@@ -114,14 +115,42 @@ def ensemble_candidates(M, n_runs):
     return out
 
 
-def tune_ensemble(kind, length, ps, n_runs, precision='fp32', micro=True, model='bond',
-                  cache_path=DEFAULT_CACHE, candidates=None, key=5, reps=2):
-    """Best launch shapes {'uf_block', 'm2_tile', 'reduce_slices', 'window'}
-    for one ensemble step of n_runs runs of this lattice and p grid, and the
-    table of all timings (the best of `reps` steps per candidate, after one
-    untimed warm-up step): {'best': {...}, 'table': [({...}, ms), ...]}."""
+def _time_ensemble(kind, length, ps, n_runs, precision, micro, model, cand, key, reps, warm=False):
+    """Best of `reps` CUDA-event timings (ms) of one ensemble step with the
+    launch shapes `cand` (after an untimed step when `warm`: a process's
+    first steps run slower -- module loading, cold TLBs)."""
     from .ensemble import Ensemble
     torch = nat.torch_cuda()
+    stream = torch.cuda.current_stream()
+    ens = Ensemble(kind, length, ps, precision=precision, micro=micro, window=cand['window'],
+                   model=model, tuning=cand)
+    ens._ws = nat.device_empty(ens.workspace_bytes(n_runs))  # allocated outside the timing
+    if warm:
+        ens.run(n_runs, key=key, run0=0)
+    best_ms = None
+    for rep in range(reps):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ens.run(n_runs, key=key, run0=(rep + 1) * n_runs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best_ms = ms if best_ms is None else min(best_ms, ms)
+    del ens
+    torch.cuda.empty_cache()
+    return best_ms
+
+
+def tune_ensemble(kind, length, ps, n_runs, precision='fp32', micro=True, model='bond',
+                  cache_path=DEFAULT_CACHE, candidates=None, key=5, reps=2):
+    """Best launch shapes {'uf_block', 'm2_tile', 'conv_tile', 'taper',
+    'reduce_slices', 'window'} for one ensemble step of n_runs runs of this
+    lattice and p grid, and the table of all timings (the best of `reps`
+    steps per candidate, after one untimed warm-up step; the last row
+    combines every single change that beat the defaults):
+    {'best': {...}, 'table': [({...}, ms), ...]}."""
     ps = np.asarray(ps, dtype=np.float64)
     spec = ('ensemble', kind, int(length), model, len(ps), float(ps.min()), float(ps.max()),
             int(n_runs), precision, bool(micro))
@@ -136,31 +165,24 @@ def tune_ensemble(kind, length, ps, n_runs, precision='fp32', micro=True, model=
         hit = cache[ck]
         return {'best': hit['best'], 'table': hit['table'], 'cached': True}
     table = []
-    stream = torch.cuda.current_stream()
     from .ensemble import lattice_kind
     from .hpc import GraphSpec
     M = GraphSpec(lattice_kind(kind, model), int(length)).M
     cands = candidates or ensemble_candidates(M, n_runs)
     for i, cand in enumerate(cands):
-        ens = Ensemble(kind, length, ps, precision=precision, micro=micro, window=cand['window'],
-                       model=model, tuning=cand)
-        ens._ws = nat.device_empty(ens.workspace_bytes(n_runs))  # allocated outside the timing
-        if i == 0:  # the process's first steps run slower (module loading, cold TLBs)
-            ens.run(n_runs, key=key, run0=0)
-        best_ms = None
-        for rep in range(reps):
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            ens.run(n_runs, key=key, run0=(rep + 1) * n_runs)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
-            best_ms = ms if best_ms is None else min(best_ms, ms)
-        table.append((dict(cand), best_ms))
-        del ens
-        torch.cuda.empty_cache()
+        table.append((dict(cand), _time_ensemble(kind, length, ps, n_runs, precision, micro, model,
+                                                 cand, key, reps, warm=(i == 0))))
+    if candidates is None and len(table) > 1:
+        # the candidates change one shape at a time: also time every change
+        # that beat the defaults, together
+        base, base_ms = table[0]
+        combo = dict(base)
+        for cand, ms in sorted(table[1:], key=lambda t: -t[1]):  # the best change last
+            if ms < base_ms:
+                combo.update({k: v for k, v in cand.items() if v != base[k]})
+        if combo not in [c for c, _ in table]:
+            table.append((combo, _time_ensemble(kind, length, ps, n_runs, precision, micro, model,
+                                                combo, key, reps)))
     best = min(table, key=lambda t: t[1])[0]
     result = {'best': best, 'table': table, 'cached': False}
     if cache_path:

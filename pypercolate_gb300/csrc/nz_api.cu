@@ -298,7 +298,8 @@ int nz_canonical_statistics_records(const NzRecords *rec, uint32_t num_nodes, ui
     p.w32 = nullptr;
     p.w32lo = nullptr;
     p.core_lo = p.core_len = nullptr;
-    p.m2_tile = 16;
+    p.m2_tile = 8;
+    p.conv_tile = 8;
     p.acc = out;
     p.errors = nullptr;
     launch_conv_window(p, 0, s);
@@ -563,14 +564,16 @@ int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning, int32_t n_runs, ui
                       const NzTuning *tuning, void *workspace, size_t workspace_bytes, uint64_t *acc_count,
                       double *acc_mean, double *acc_m2, const NzMicroAccum *micro, void *stream) {
     if (!graph || n_runs <= 0 || P <= 0 || !ps || !acc_count || !acc_mean || !acc_m2) return NZ_ERR_INVALID;
-    int32_t uf_block = 128, m2_tile = 16, slices = 0;
+    int32_t uf_block = 128, m2_tile = 8, slices = 0, conv_tile = 8, taper = 0;
     if (tuning) {
         if (tuning->uf_block) uf_block = tuning->uf_block;
         if (tuning->m2_tile) m2_tile = tuning->m2_tile;
+        if (tuning->conv_tile) conv_tile = tuning->conv_tile;
         slices = tuning->reduce_slices;
+        taper = tuning->taper != 0;
     }
-    if ((uf_block != 32 && uf_block != 64 && uf_block != 128) || (m2_tile != 8 && m2_tile != 16) || slices < 0 ||
-        slices > kMaxSlices)
+    if ((uf_block != 32 && uf_block != 64 && uf_block != 128) || (m2_tile != 8 && m2_tile != 16) ||
+        (conv_tile != 8 && conv_tile != 16) || slices < 0 || slices > kMaxSlices)
         return NZ_ERR_INVALID;
     if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
     if (!(cutoff > 0)) cutoff = kDefaultCutoff;
@@ -635,6 +638,7 @@ int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning, int32_t n_runs, ui
     cp.core_lo = L.core_lo32;
     cp.core_len = L.core_len32;
     cp.m2_tile = m2_tile;
+    cp.conv_tile = conv_tile;
     cp.acc = L.stats;
     cp.errors = L.flag + 1;  // with the union-find's corruption count
     MicroParams mp;
@@ -652,8 +656,23 @@ int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning, int32_t n_runs, ui
     // its union-find.  Node words and run state live on `s` only, the
     // accumulators on s2 only.
     int k = 0;
-    for (uint32_t w0 = 0; w0 <= M; w0 += (uint32_t)L.window, ++k) {
-        const uint32_t w1 = (w0 + (uint32_t)L.window > M + 1) ? M + 1 : w0 + (uint32_t)L.window;
+    // Window schedule.  Only the first window's union-find runs with no
+    // consumer beside it, and only the last window's consumers with no
+    // union-find: with `taper` those two windows are a quarter window long
+    // (at least 256 rows), the rest full.
+    const uint32_t W = (uint32_t)L.window;
+    const uint32_t q = taper ? (W / 4 > 256u ? W / 4 : (W < 256u ? W : 256u)) : W;
+    auto window_end = [&](uint32_t w0, int kk) -> uint32_t {
+        uint32_t len = W;
+        if (taper) {
+            const uint32_t rem = M + 1 - w0;
+            if (kk == 0) len = q;
+            else if (rem > W && rem < W + q) len = rem - q;  // leave a short last window
+        }
+        return (w0 + len > M + 1) ? M + 1 : w0 + len;
+    };
+    for (uint32_t w0 = 0, w1 = 0; w0 <= M; w0 = w1, ++k) {
+        w1 = window_end(w0, k);
         const int b = k & 1;
         if (k >= 2 && cudaStreamWaitEvent(s, aux.a->consumed[b], 0) != cudaSuccess) return NZ_ERR_CUDA;
         up.rec = L.rec[b];

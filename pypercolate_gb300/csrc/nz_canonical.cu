@@ -264,11 +264,11 @@ void launch_band_dot(const uint32_t *band_lo, const uint32_t *band_len, const do
 // =====================================================================
 // Banded convolution of record windows (ensemble path)
 // =====================================================================
-#ifndef NZ_CONV_PT
-#define NZ_CONV_PT 8
-#endif
 constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
-constexpr int kConvPT = NZ_CONV_PT;    // probabilities per CTA
+// probabilities per CTA of the FP32 / FP64 window kernels: 8 by default
+// (round 1: 8 gave 544 ms, 16 587 ms, 32 1025 ms per 100,000-run step with
+// the FP64-accumulated kernels); 16 is an autotuner candidate
+constexpr int kConvPT = 8;
 constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before the TwoSum add
 // 16 record loads in flight per thread: over the FP32 band (weights >= e^-30
 // of the mode) 1047 against 1052 ms per 100,000-run L = 256 step with 8
@@ -309,7 +309,7 @@ struct ConvAcc<1> {
 // p's band).  PRECISION 0: FP64 products and sums.  PRECISION 1: FP32
 // products summed in FP32 over kConvChunk rows, then added into a TwoSum
 // pair (ConvAcc<1>).
-template <int PRECISION, int S, bool SITE>
+template <int PRECISION, int S, bool SITE, int kConvPT>
 __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                           const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
                                           ConvAcc<PRECISION> *acc) {
@@ -351,7 +351,7 @@ __device__ __forceinline__ void conv_rows(const ConvParams &p, uint32_t c0, uint
 // max_span plane: one pass loads each word once and feeds the three sets of
 // products (each accumulator adds the same values in the same order as a
 // pass per statistic would).
-template <int PRECISION, bool SITE>
+template <int PRECISION, bool SITE, int kConvPT>
 __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, uint32_t cn, int r,
                                               const typename std::conditional<PRECISION == 0, double, float>::type (*s_w)[kConvPT],
                                               ConvAcc<PRECISION> *acc0, ConvAcc<PRECISION> *acc1,
@@ -405,7 +405,7 @@ __device__ __forceinline__ void conv_rows_max(const ConvParams &p, uint32_t c0, 
 #else
 #define NZ_CONV_BOUNDS __launch_bounds__(kConvRuns)
 #endif
-template <int PRECISION, bool SITE, bool MAXSET>
+template <int PRECISION, bool SITE, bool MAXSET, int kConvPT>
 __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
     using wtype = typename std::conditional<PRECISION == 0, double, float>::type;
     __shared__ wtype s_w[kConvChunk][kConvPT];
@@ -451,21 +451,21 @@ __global__ void NZ_CONV_BOUNDS conv_window_kernel(ConvParams p) {
         __syncthreads();
         if (r < p.n_runs) {
             if (MAXSET) {
-                conv_rows_max<PRECISION, SITE>(p, c0, cn, r, s_w, acc0, acc, acc3);
+                conv_rows_max<PRECISION, SITE, kConvPT>(p, c0, cn, r, s_w, acc0, acc, acc3);
             } else {
                 switch (s) {
                     case 2:
-                        if (p.rec.narrow) conv_rows<PRECISION, 8, SITE>(p, c0, cn, r, s_w, acc);
-                        else conv_rows<PRECISION, 2, SITE>(p, c0, cn, r, s_w, acc);
+                        if (p.rec.narrow) conv_rows<PRECISION, 8, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 2, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
                         break;
                     case 4:
-                        if (p.rec.narrow) conv_rows<PRECISION, 9, SITE>(p, c0, cn, r, s_w, acc);
-                        else conv_rows<PRECISION, 4, SITE>(p, c0, cn, r, s_w, acc);
+                        if (p.rec.narrow) conv_rows<PRECISION, 9, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 4, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
                         break;
-                    case 5: conv_rows<PRECISION, 5, SITE>(p, c0, cn, r, s_w, acc); break;
+                    case 5: conv_rows<PRECISION, 5, SITE, kConvPT>(p, c0, cn, r, s_w, acc); break;
                     default:
-                        if (p.rec.m4_hi) conv_rows<PRECISION, 6, SITE>(p, c0, cn, r, s_w, acc);
-                        else conv_rows<PRECISION, 7, SITE>(p, c0, cn, r, s_w, acc);
+                        if (p.rec.m4_hi) conv_rows<PRECISION, 6, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
+                        else conv_rows<PRECISION, 7, SITE, kConvPT>(p, c0, cn, r, s_w, acc);
                         break;
                 }
             }
@@ -554,10 +554,10 @@ __device__ __forceinline__ void split_u32(uint32_t q, float &qh, float &ql) {
 // tile's probabilities runs the compensated arithmetic on all its rows
 // (branch-free, so the kM2PT accumulator chains interleave); a chunk
 // entirely in the tails runs plain FP32 products.
-// kM2PT probabilities per CTA (the tuned m2_tile, 8 or 16; 16 by default:
-// each loaded record then feeds twice the compensated arithmetic of an
-// 8-probability tile, 1128 against 1218 ms per 100,000-run L = 256 step;
-// 32 measured 1285 ms)
+// kM2PT probabilities per CTA (the tuned m2_tile, 8 or 16; 8 by default:
+// on the same box 8 gave 1085.8 and 1204.7 ms per 100,000-run L = 256 step
+// against 1108.8 and 1224.7 ms for 16 (two boxes); 32 measured 1285 against
+// 1128 ms for 16)
 template <bool NARROW, int kM2PT>
 __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
     __shared__ float s_wh[kConvChunk][kM2PT], s_wl[kConvChunk][kM2PT];
@@ -667,7 +667,7 @@ __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
 
 void launch_conv_m2_comp(const ConvParams &p, cudaStream_t s) {
     if (p.n_runs <= 0 || p.P <= 0) return;
-    const int pt = p.m2_tile == 8 ? 8 : 16;
+    const int pt = p.m2_tile == 16 ? 16 : 8;
     dim3 g((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + pt - 1) / pt, 1);
     if (pt == 8) {
         if (p.rec.narrow) conv_m2_comp_kernel<true, 8><<<g, kConvRuns, 0, s>>>(p);
@@ -683,33 +683,41 @@ bool conv_grid_fits(int32_t n_runs, int32_t P) {
     return n_runs > 0 && P > 0 && (P + kConvPT - 1) / kConvPT <= 65535;
 }
 
-void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
-    if (p.n_runs <= 0 || p.P <= 0) return;
+template <int PT>
+static void launch_conv_window_pt(const ConvParams &p, int precision, cudaStream_t s) {
     // (run tiles, p tiles, statistics); launching the p tiles of one run tile
     // back to back (for L2 reuse of its records) measured slower
-    dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
+    dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + PT - 1) / PT, 1);
     dim3 gother(gmax.x, gmax.y, precision == 0 ? 4 : 3);
     // the record model is a template parameter: a run-time test in the row
     // loop cost 17 % of the kernel's time
     if (p.rec.site) {
         if (precision == 0) {
-            conv_window_kernel<0, true, true><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<0, true, false><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, true, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, true, false, PT><<<gother, kConvRuns, 0, s>>>(p);
         } else {
-            conv_window_kernel<1, true, true><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<1, true, false><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, true, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, true, false, PT><<<gother, kConvRuns, 0, s>>>(p);
             launch_conv_m2_comp(p, s);
         }
     } else {
         if (precision == 0) {
-            conv_window_kernel<0, false, true><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<0, false, false><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, false, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, false, false, PT><<<gother, kConvRuns, 0, s>>>(p);
         } else {
-            conv_window_kernel<1, false, true><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<1, false, false><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, false, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, false, false, PT><<<gother, kConvRuns, 0, s>>>(p);
             launch_conv_m2_comp(p, s);
         }
     }
+}
+
+void launch_conv_window(const ConvParams &p, int precision, cudaStream_t s) {
+    if (p.n_runs <= 0 || p.P <= 0) return;
+    // the FP64 path keeps 8 probabilities per CTA (its accumulators are
+    // twice as wide)
+    if (precision != 0 && p.conv_tile == 16) launch_conv_window_pt<16>(p, precision, s);
+    else launch_conv_window_pt<kConvPT>(p, precision, s);
 }
 
 // Weights of the FP32 convolution: the part of each p's band whose weights

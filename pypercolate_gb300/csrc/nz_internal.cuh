@@ -66,6 +66,7 @@ struct ConvParams {
     const float *w32lo;      // [P][cap] w64 - w32 as FP32 (the compensated m2 products)
     const uint32_t *core_lo, *core_len;  // rows whose weight is >= e^-8 of the mode (m2 compensated)
     int32_t m2_tile;         // probabilities per CTA of the compensated m2 kernel (8 or 16)
+    int32_t conv_tile;       // probabilities per CTA of the FP32 window kernels (8 or 16)
     double *acc;             // [n_runs][P][7], accumulated (+=)
     uint32_t *errors;        // tensor-core path: counts CTAs whose waits gave up (or null)
 };

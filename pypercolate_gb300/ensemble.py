@@ -54,8 +54,8 @@ class Ensemble:
               sums per 32-row chunk added into TwoSum pairs) or 'fp64'
     micro     also accumulate microcanonical run-reductions for every n
     window    rows per union-find launch (0: sized to ~32 GiB of records per window)
-    tuning    launch shapes {'uf_block', 'm2_tile', 'reduce_slices'} (autotune.tune_ensemble
-              picks them; None: the library's defaults)
+    tuning    launch shapes {'uf_block', 'm2_tile', 'reduce_slices', 'conv_tile', 'taper'}
+              (autotune.tune_ensemble picks them; None: the library's defaults)
     """
 
     def __init__(self, kind='grid', length=16, ps=None, spanning=True, precision='fp32',
@@ -118,7 +118,9 @@ class Ensemble:
         tune = None
         if self.tuning:
             tune = nat.NzTuning(int(self.tuning.get('uf_block', 0)), int(self.tuning.get('m2_tile', 0)),
-                                int(self.tuning.get('reduce_slices', 0)))
+                                int(self.tuning.get('reduce_slices', 0)),
+                                int(self.tuning.get('conv_tile', 0)),
+                                int(self.tuning.get('taper', 0)))
         st = lib.nz_ensemble_tuned(g, int(self.spanning), n_runs, int(key), int(run0),
                                    nat.ptr(self.d_ps), self.P, self.cutoff, self.window,
                                    self.precision, tune, nat.ptr(self._ws), self._ws.numel(),

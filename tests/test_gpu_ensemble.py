@@ -269,3 +269,31 @@ def test_square_grid_spans_half_the_time_at_one_half(gpu):
     ens.run(R, key=99, run0=0)
     got = float(ens.canonical_averages()['percolation_probability_mean'][0])
     assert abs(got - 0.5) < 5 * np.sqrt(0.25 / R) + 0.02, got
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'tf32x3'])
+def test_tuned_launch_shapes_give_the_same_results(gpu, precision):
+    """Every launch shape the autotuner can pick (runs per union-find CTA,
+    probability tiles of the two FP32 convolutions, run-reduction slices,
+    record window and its tapered schedule) gives the same ensemble: exact micro sums equal, canonical
+    curves equal to FP32 rounding of the per-run sums (1e-6 relative)."""
+    from pypercolate_gb300.ensemble import Ensemble
+    ps = np.linspace(0.0, 1.0, 61)
+    L, R = 20, 700
+    ref = Ensemble('grid', L, ps, precision=precision, micro=True)
+    ref.run(R, key=21, run0=3)
+    want = ref.canonical_averages()
+    for tuning, window in (({'uf_block': 64, 'conv_tile': 16, 'm2_tile': 8, 'reduce_slices': 256}, 97),
+                           ({'uf_block': 32, 'conv_tile': 16, 'm2_tile': 16, 'reduce_slices': 1,
+                             'taper': 1}, 0),
+                           ({'taper': 1}, 300)):
+        ens = Ensemble('grid', L, ps, precision=precision, micro=True, window=window, tuning=tuning)
+        ens.run(R, key=21, run0=3)
+        assert ens.errors() == 0
+        got = ens.canonical_averages()
+        for k in ('percolation_probability_mean', 'max_cluster_size_mean', 'moments_mean'):
+            np.testing.assert_allclose(got[k], want[k], rtol=1e-6, atol=1e-9)
+        a, b = ens.micro_sums(), ref.micro_sums()
+        assert a['count'] == b['count'] == R
+        assert (a['sums'] == b['sums']).all()
+        assert np.array_equal(a['span_count'], b['span_count'])

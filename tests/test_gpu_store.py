@@ -140,3 +140,26 @@ def test_host_merge_of_states_matches_device_merge(gpu):
     for k in ('count', 'span_count', 'sum_lo', 'sum_hi'):
         assert np.array_equal(np.asarray(got['micro'][k]), np.asarray(want['micro'][k])), k
     np.testing.assert_allclose(got['micro']['m2'], want['micro']['m2'], rtol=1e-14, atol=1e-9)
+
+
+def test_merged_ensemble_of_one_rank_is_the_rank_itself(gpu):
+    """distributed.merged_ensemble -- the gather and device merge that a
+    multi-GPU job runs once after its runs -- in a one-rank gloo group gives
+    back the rank's own state bit for bit (the N > 1 exchange is covered on
+    CPU by tests/test_distributed.py)."""
+    import socket
+    import torch.distributed as dist
+    from pypercolate_gb300.distributed import merged_ensemble
+    sock = socket.socket()
+    sock.bind(('127.0.0.1', 0))
+    port = sock.getsockname()[1]
+    sock.close()
+    dist.init_process_group('gloo', init_method='tcp://127.0.0.1:%d' % port, rank=0, world_size=1)
+    try:
+        ens = make()
+        ens.run(150, key=9, run0=0)
+        merged = merged_ensemble(ens)
+        assert bits(merged) == bits(ens)
+        assert merged.ledger == ens.ledger
+    finally:
+        dist.destroy_process_group()

@@ -554,6 +554,14 @@ __device__ __forceinline__ void split_u32(uint32_t q, float &qh, float &ql) {
 // tile's probabilities runs the compensated arithmetic on all its rows
 // (branch-free, so the kM2PT accumulator chains interleave); a chunk
 // entirely in the tails runs plain FP32 products.
+// record loads in flight per thread of the compensated m2 kernel: 32
+// against 16, 1092 against 1099 ms per 100,000-run L = 256 step (same box,
+// the convolution stream 801 against 838 ms)
+#ifndef NZ_M2_BATCH
+#define NZ_M2_BATCH 32
+#endif
+constexpr int kM2Batch = NZ_M2_BATCH;
+
 // kM2PT probabilities per CTA (the tuned m2_tile, 8 or 16; 8 by default:
 // on the same box 8 gave 1085.8 and 1204.7 ms per 100,000-run L = 256 step
 // against 1108.8 and 1224.7 ms for 16 (two boxes); 32 measured 1285 against
@@ -608,45 +616,52 @@ __global__ void NZ_CONV_BOUNDS conv_m2_comp_kernel(ConvParams p) {
         __syncthreads();
         if (r >= p.n_runs) continue;
         const size_t base = (size_t)(c0 - p.n_begin) * p.rec.run_stride + r;
-        auto load = [&](uint32_t i, float &qh, float &ql) {
-            const size_t off = base + (size_t)i * p.rec.run_stride;
-            if (NARROW) split_u32(m2n[off], qh, ql);
-            else split_u64(p.rec.m2[off], qh, ql);
+        // raw m2 words of kM2Batch rows are loaded before any is split and
+        // used, so that many loads are in flight per thread
+        using raw_t = typename std::conditional<NARROW, uint32_t, uint64_t>::type;
+        const raw_t *plane = NARROW ? reinterpret_cast<const raw_t *>(m2n)
+                                    : reinterpret_cast<const raw_t *>(p.rec.m2);
+        auto split = [&](raw_t w, float &qh, float &ql) {
+            if constexpr (NARROW) split_u32(w, qh, ql);
+            else split_u64(w, qh, ql);
         };
         uint32_t i = 0;
         if (core) {
-            for (; i + kConvBatch <= cn; i += kConvBatch) {
-                float qh[kConvBatch], ql[kConvBatch];
+            for (; i + kM2Batch <= cn; i += kM2Batch) {
+                raw_t w[kM2Batch];
 #pragma unroll
-                for (int b = 0; b < kConvBatch; ++b) load(i + b, qh[b], ql[b]);
+                for (int b = 0; b < kM2Batch; ++b) w[b] = plane[base + (size_t)(i + b) * p.rec.run_stride];
 #pragma unroll
-                for (int b = 0; b < kConvBatch; ++b)
+                for (int b = 0; b < kM2Batch; ++b) {
+                    float qh, ql;
+                    split(w[b], qh, ql);
 #pragma unroll
-                    for (int j = 0; j < kM2PT; ++j) acc[j].add(s_wh[i + b][j], s_wl[i + b][j], qh[b], ql[b]);
+                    for (int j = 0; j < kM2PT; ++j) acc[j].add(s_wh[i + b][j], s_wl[i + b][j], qh, ql);
+                }
             }
             for (; i < cn; ++i) {
                 float qh, ql;
-                load(i, qh, ql);
+                split(plane[base + (size_t)i * p.rec.run_stride], qh, ql);
 #pragma unroll
                 for (int j = 0; j < kM2PT; ++j) acc[j].add(s_wh[i][j], s_wl[i][j], qh, ql);
             }
         } else {
-            for (; i + kConvBatch <= cn; i += kConvBatch) {
-                float q[kConvBatch];
+            for (; i + kM2Batch <= cn; i += kM2Batch) {
+                raw_t w[kM2Batch];
 #pragma unroll
-                for (int b = 0; b < kConvBatch; ++b) {
+                for (int b = 0; b < kM2Batch; ++b) w[b] = plane[base + (size_t)(i + b) * p.rec.run_stride];
+#pragma unroll
+                for (int b = 0; b < kM2Batch; ++b) {
                     float qh, ql;
-                    load(i + b, qh, ql);
-                    q[b] = __fadd_rn(qh, ql);
+                    split(w[b], qh, ql);
+                    const float q = __fadd_rn(qh, ql);
+#pragma unroll
+                    for (int j = 0; j < kM2PT; ++j) acc[j].add_tail(s_wh[i + b][j], q);
                 }
-#pragma unroll
-                for (int b = 0; b < kConvBatch; ++b)
-#pragma unroll
-                    for (int j = 0; j < kM2PT; ++j) acc[j].add_tail(s_wh[i + b][j], q[b]);
             }
             for (; i < cn; ++i) {
                 float qh, ql;
-                load(i, qh, ql);
+                split(plane[base + (size_t)i * p.rec.run_stride], qh, ql);
                 const float q = __fadd_rn(qh, ql);
 #pragma unroll
                 for (int j = 0; j < kM2PT; ++j) acc[j].add_tail(s_wh[i][j], q);

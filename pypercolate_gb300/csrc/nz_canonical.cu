@@ -272,7 +272,8 @@ constexpr int kConvPT = 8;
 constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before the TwoSum add
 // 16 record loads in flight per thread: over the FP32 band (weights >= e^-30
 // of the mode) 1047 against 1052 ms per 100,000-run L = 256 step with 8
-// (over the full e^-80 band 8 had been better: 479 against 512 ms)
+// (over the full e^-80 band 8 had been better: 479 against 512 ms); 32
+// measured 1229 against 1211 ms (same box)
 #ifndef NZ_CONV_BATCH
 #define NZ_CONV_BATCH 16
 #endif
@@ -1001,9 +1002,12 @@ __device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
 #ifndef NZ_MICRO_MIN_BLOCKS
 #define NZ_MICRO_MIN_BLOCKS 3
 #endif
-#ifndef NZ_MICRO_PAIR
-#define NZ_MICRO_PAIR 1
+// records in flight per thread: 2 against 1 took the kernel from 400 to
+// 179 ms per 100,000-run L = 256 step inside the pipeline
+#ifndef NZ_MICRO_INFLIGHT
+#define NZ_MICRO_INFLIGHT 2
 #endif
+constexpr int kMicroInflight = NZ_MICRO_INFLIGHT;
 #define NZ_MICRO_BOUNDS __launch_bounds__(BLOCK, NZ_MICRO_MIN_BLOCKS)
 
 // One block per row n: reduces all statistics of that row over the runs and
@@ -1066,16 +1070,16 @@ __global__ void NZ_MICRO_BOUNDS micro_window_kernel(MicroParams p) {
         scaled_split((uint64_t)ad4, (uint64_t)(ad4 >> 64), e4, yh, yl);
         add_square(a.fs_m4, a.fc_m4, yh, yl);
     };
-    // NZ_MICRO_PAIR: the records of two runs are loaded before either is
-    // added, so each thread keeps two records' loads in flight
+    // the records of NZ_MICRO_INFLIGHT runs are loaded before any is added,
+    // so each thread keeps that many records' loads in flight
     int r = threadIdx.x;
-#if NZ_MICRO_PAIR
-    for (; r + BLOCK < p.n_runs; r += 2 * BLOCK) {
-        const Rec q0 = load(r), q1 = load(r + BLOCK);
-        add(q0);
-        add(q1);
+    for (; r + (kMicroInflight - 1) * BLOCK < p.n_runs; r += kMicroInflight * BLOCK) {
+        Rec q[kMicroInflight];
+#pragma unroll
+        for (int k = 0; k < kMicroInflight; ++k) q[k] = load(r + k * BLOCK);
+#pragma unroll
+        for (int k = 0; k < kMicroInflight; ++k) add(q[k]);
     }
-#endif
     for (; r < p.n_runs; r += BLOCK) add(load(r));
     // block sums (results valid in thread 0)
     const uint64_t span = bsum_u64<BLOCK>(a.span, s_w);

@@ -318,11 +318,15 @@ int nz_mt_stream_permutations(const uint32_t *state_in, uint32_t num_edges,
  * -> banded canonical convolution at P probabilities -> pairwise merge.
  * Results are merged into (acc_count, acc_mean[P*7], acc_m2[P*7]) and, if
  * micro != NULL, into *micro.  conv_precision: 0 = FP64 over each band
- * of `cutoff` (log B >= log B(mode) - cutoff); 1 = FP32 products with FP64
- * chunk accumulation over the rows of the band whose weights are >= e^-30 x
- * the mode's (the weights left out sum to < 1e-13); 2 = the same rows on
- * the tensor cores (tcgen05 kind::tf32, three split products per term,
- * FP32 chunk sums added into TwoSum pairs).  A convolution wait that gives
+ * of `cutoff` (log B >= log B(mode) - cutoff); 1 = FP32 products summed in
+ * FP32 over 128-row chunks and carried as FP32 (sum, compensation) pairs,
+ * over the rows of the band whose weights are >= e^-30 x the mode's (the
+ * weights left out sum to < 1e-13); 2 = the same rows on the tensor cores
+ * (tcgen05 kind::tf32, three split products per term).  In 1 and 2 the m2
+ * statistic (the susceptibility) runs on a compensated FP32 kernel (FP32 hi +
+ * lo weights, exact two-part values, error-free products and sums over the
+ * band's core), ~2^-44 relative per run, so that its curve stays within
+ * 1e-6 absolute of FP64 where it reaches ~1e4.  A convolution wait that gives
  * up is counted with nz_ensemble_errors.  The union-find runs on `stream`; the reductions
  * and the convolution of each window of records run on a second stream of
  * the library's (one per concurrent call and device, created on first use

@@ -579,8 +579,13 @@ def main():
     # second ceiling for the union-find: HBM's rate of scattered sector reads
     gather_rate = random_gather_rate()
     uf_adds_per_s = adds_per_launch / uf_avg_s
-    kernels_per_seq = {'setup': 4, 'union_find': 1, 'micro': 1,
-                       'conv': 1 if args.precision == 'tf32x3' else 2, 'reduce': 4}
+    # kernels per profiled launch sequence: set-up (band weights, FP32
+    # weights, node and state initialisation), union-find, micro reductions,
+    # convolution (FP32: max-set, other statistics, compensated m2; tf32x3:
+    # tcgen05 kernel, compensated m2; FP64: max-set, other statistics),
+    # reduction (micro count, two run-reduction passes, count)
+    kernels_per_seq = {'setup': 3 if args.precision == 'fp64' else 4, 'union_find': 1, 'micro': 1,
+                       'conv': {'fp32': 3, 'tf32x3': 2, 'fp64': 2}[args.precision], 'reduce': 4}
     gpu_launches = int(sum(launches[k] * kernels_per_seq[k] for k in launches))
 
     # per-curve error of the timed arithmetic against FP64, on a sample of

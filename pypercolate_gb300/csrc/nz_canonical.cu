@@ -1003,7 +1003,9 @@ __device__ __forceinline__ uint64_t bsum_u64(uint64_t v, uint64_t *s_tmp) {
 #define NZ_MICRO_MIN_BLOCKS 3
 #endif
 // records in flight per thread: 2 against 1 took the kernel from 400 to
-// 179 ms per 100,000-run L = 256 step inside the pipeline
+// 179 ms per 100,000-run L = 256 step inside the pipeline; 4 (with a few
+// hundred bytes of spills at the 80-register cap) gave the same step time
+// (1076.2 against 1076.0 ms, same box)
 #ifndef NZ_MICRO_INFLIGHT
 #define NZ_MICRO_INFLIGHT 2
 #endif

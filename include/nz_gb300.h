@@ -357,7 +357,7 @@ int nz_ensemble(const NzGraph *graph, int32_t spanning, int32_t n_runs,
  * m2_tile: probabilities per CTA of the compensated m2 convolution (8 or 16;
  * 8); reduce_slices: slices of runs of the canonical run reduction (1 ..
  * 256; 1, 16 or 64 by run count); conv_tile: probabilities per CTA of the
- * FP32 convolution kernels of the other statistics (8 or 16; 8); taper: 1 =
+ * FP32 convolution kernel of m0, m3 and m4 (8 or 16; 8); taper: 1 =
  * the first and the last record window a quarter window long (the first
  * window's union-find and the last window's reductions run alone), 0 = all
  * windows full (0).  The record window is nz_ensemble's `window`.  No

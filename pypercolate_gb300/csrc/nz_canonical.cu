@@ -699,30 +699,33 @@ bool conv_grid_fits(int32_t n_runs, int32_t P) {
     return n_runs > 0 && P > 0 && (P + kConvPT - 1) / kConvPT <= 65535;
 }
 
-template <int PT>
+// PT_OTHER: probabilities per CTA of the other statistics' kernel (m0, m3,
+// m4: 18 of the 26 record bytes at L = 256); the max-set kernel keeps 8 (16
+// takes it to 201 registers beside the union-find)
+template <int PT_OTHER>
 static void launch_conv_window_pt(const ConvParams &p, int precision, cudaStream_t s) {
     // (run tiles, p tiles, statistics); launching the p tiles of one run tile
     // back to back (for L2 reuse of its records) measured slower
-    dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + PT - 1) / PT, 1);
-    dim3 gother(gmax.x, gmax.y, precision == 0 ? 4 : 3);
+    dim3 gmax((p.n_runs + kConvRuns - 1) / kConvRuns, (p.P + kConvPT - 1) / kConvPT, 1);
+    dim3 gother(gmax.x, (p.P + PT_OTHER - 1) / PT_OTHER, precision == 0 ? 4 : 3);
     // the record model is a template parameter: a run-time test in the row
     // loop cost 17 % of the kernel's time
     if (p.rec.site) {
         if (precision == 0) {
-            conv_window_kernel<0, true, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<0, true, false, PT><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, true, true, kConvPT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, true, false, kConvPT><<<gother, kConvRuns, 0, s>>>(p);
         } else {
-            conv_window_kernel<1, true, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<1, true, false, PT><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, true, true, kConvPT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, true, false, PT_OTHER><<<gother, kConvRuns, 0, s>>>(p);
             launch_conv_m2_comp(p, s);
         }
     } else {
         if (precision == 0) {
-            conv_window_kernel<0, false, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<0, false, false, PT><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, false, true, kConvPT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<0, false, false, kConvPT><<<gother, kConvRuns, 0, s>>>(p);
         } else {
-            conv_window_kernel<1, false, true, PT><<<gmax, kConvRuns, 0, s>>>(p);
-            conv_window_kernel<1, false, false, PT><<<gother, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, false, true, kConvPT><<<gmax, kConvRuns, 0, s>>>(p);
+            conv_window_kernel<1, false, false, PT_OTHER><<<gother, kConvRuns, 0, s>>>(p);
             launch_conv_m2_comp(p, s);
         }
     }

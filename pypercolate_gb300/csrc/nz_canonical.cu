@@ -266,8 +266,9 @@ void launch_band_dot(const uint32_t *band_lo, const uint32_t *band_len, const do
 // =====================================================================
 constexpr int kConvRuns = 128;         // runs per CTA (one per thread)
 // probabilities per CTA of the FP32 / FP64 window kernels: 8 by default
-// (round 1: 8 gave 544 ms, 16 587 ms, 32 1025 ms per 100,000-run step with
-// the FP64-accumulated kernels); 16 is an autotuner candidate
+// (8 gave 544 ms, 16 587 ms, 32 1025 ms per 100,000-run step with the
+// earlier FP64-accumulated kernels); 16 is an autotuner candidate for the
+// m0 / m3 / m4 kernel
 constexpr int kConvPT = 8;
 constexpr int kConvChunk = 128;  // rows staged per step, summed in FP32 before the TwoSum add
 // 16 record loads in flight per thread: over the FP32 band (weights >= e^-30

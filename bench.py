@@ -167,6 +167,8 @@ def parse():
     ap.add_argument('--plain-runs', type=int, default=8192,
                     help='runs timed on the plain path (0: skip)')
     ap.add_argument('--plain-chunk', type=int, default=4096)
+    ap.add_argument('--surrogate-steps', type=int, default=30000,
+                    help='Adam steps of --study surrogate')
     ap.add_argument('--no-tune', dest='tune', action='store_false',
                     help='skip the launch-shape autotuner of the main leg (library defaults)')
     ap.add_argument('--no-plain-mix', dest='plain_mix', action='store_false',
@@ -421,7 +423,7 @@ def surrogate_study(args):
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     model = S.MLP(seed=0)
-    steps, batch = 30000, 4096
+    steps, batch = args.surrogate_steps, 4096
     t0 = time.perf_counter()
     trace = model.fit(X, Y, steps=steps, batch=batch, lr=1e-3, log_every=1000, decay=0.05)
     torch.cuda.synchronize()

@@ -92,11 +92,12 @@ def curve_errors_vs_fp64(L, ps, precision, sample, run0, window):
             'curves': out}
 
 
-def plain_mix_leg(counts, stream, grid=(8, 512), chain=(1024, 65536), grid_step=32,
+def plain_mix_leg(counts, stream, fused=False, grid=(8, 512), chain=(1024, 65536), grid_step=32,
                   chain_step=512):
     """The uneven workload the plain way: one lattice size per launch
     sequence (class draw, queue, union-find with the same 256 checkpoints,
-    exact reduction), back to back on one stream, each class with the runs
+    exact reduction, the batched leg's choice of reduction), back to back on
+    one stream, each class with the runs
     the batched ensemble gave it (`counts`, grid classes then chain
     classes).  Timed on a stratified sample -- every grid_step-th grid
     length and every chain_step-th chain length -- and scaled by the strata
@@ -109,13 +110,14 @@ def plain_mix_leg(counts, stream, grid=(8, 512), chain=(1024, 65536), grid_step=
         if counts[c]:
             L = grid[0] + c
             legs.append(('grid', grid_step, MixEnsemble(int(counts[c]), grid=(L, L), chain=chain[:1] * 2,
-                                                        chain_share=0.0, threads=int(counts[c]))))
+                                                        chain_share=0.0, threads=int(counts[c]),
+                                                        fused=fused)))
     for c in range(0, chain[1] - chain[0] + 1, chain_step):
         k = int(counts[n_grid + c])
         if k:
             l = chain[0] + c
             legs.append(('chain', chain_step, MixEnsemble(k, grid=grid[:1] * 2, chain=(l, l),
-                                                          chain_share=1.0, threads=k)))
+                                                          chain_share=1.0, threads=k, fused=fused)))
     for _, _, e in legs[:4]:  # warm-up (module load)
         e.run(1)
     torch.cuda.synchronize()
@@ -639,8 +641,8 @@ def main():
         from pypercolate_gb300.autotune import tune_mix
         from pypercolate_gb300.mix import MixEnsemble
         tuned = tune_mix(args.mix_runs, cache_path=None)
-        threads, block, smem = tuned['best']
-        me = MixEnsemble(args.mix_runs, threads=threads, block=block, smem_words=smem)
+        threads, block, smem, fused = tuned['best']
+        me = MixEnsemble(args.mix_runs, threads=threads, block=block, smem_words=smem, fused=fused)
         me.capture()
         me.replay(7)
         torch.cuda.synchronize()
@@ -656,7 +658,8 @@ def main():
         counts = me.count.cpu().numpy().astype(np.int64)
         mix = {'value': adds / (mms * 1e-3), 'unit': 'bond additions/s', 'runs': args.mix_runs,
                'additions_per_ensemble': adds, 'ms_per_ensemble': mms,
-               'launch': {'threads': threads, 'block': block, 'smem_words': smem},
+               'launch': {'threads': threads, 'block': block, 'smem_words': smem,
+                          'reduction': 'fused' if fused else 'records'},
                'autotune': [list(t) for t in tuned['table']], 'cuda_graph': True,
                'workload': '2D L log-uniform [8,512] + chains l log-uniform [1024,65536], '
                            '50/50, 256 checkpoints, exact per-lattice reductions; union-find '
@@ -665,7 +668,7 @@ def main():
         del me
         torch.cuda.empty_cache()
         if args.plain_mix:
-            mix['plain'] = plain_mix_leg(counts, stream)
+            mix['plain'] = plain_mix_leg(counts, stream, fused=fused)
             mix['batched_vs_plain'] = mix['value'] / mix['plain']['value']
 
     # end to end through the public API: inputs (p-grid) from pinned host

@@ -390,12 +390,22 @@ int nz_ensemble_tuned(const NzGraph *graph, int32_t spanning,
  * Runs of every lattice (kind, length) = "class" are reduced at `checkpoints`
  * occupation numbers n_j = floor(j M / (checkpoints - 1)), j = 0..F-1, to
  * exact integer sums and exact-numerator M2 of max, m0, m1, m2, m3, m4 and
- * spanning counts (percolate/percolate.py:450-705 statistics at those n). */
+ * spanning counts (percolate/percolate.py:450-705 statistics at those n).
+ * `reduction` picks how (identical results): NZ_MIX_REDUCE_RECORDS -- each
+ * run writes its checkpoint statistics, a second kernel reduces them per
+ * class; NZ_MIX_REDUCE_FUSED -- the union-find threads add each run's
+ * statistics and squares into its class's sums themselves (exact integer
+ * atomics), and a per-cell kernel only forms the outputs.  The fused form
+ * needs no per-run records and is faster where lattices have many runs each;
+ * the records form where they have few (the autotuner measures both). */
+#define NZ_MIX_REDUCE_RECORDS 0
+#define NZ_MIX_REDUCE_FUSED 1
 typedef struct NzMixSpec {
     uint32_t grid_min, grid_max;   /* spanning_2d_grid lengths (inclusive)   */
     uint32_t chain_min, chain_max; /* spanning_1d_chain lengths (inclusive)  */
     uint32_t chain_share;          /* P(chain) * 2^32                         */
     int32_t checkpoints;           /* F >= 2                                  */
+    int32_t reduction;             /* NZ_MIX_REDUCE_RECORDS or _FUSED        */
 } NzMixSpec;
 
 /* Per class c (grid classes first: c = L - grid_min; then chains:
@@ -411,7 +421,10 @@ typedef struct NzMixAccum {
 } NzMixAccum;
 
 /* Workspace for n_runs runs and `threads` persistent threads; each thread's
- * node slot is sized for the largest lattice of the spec. */
+ * node slot is sized for the largest lattice of the spec.  Beside the node
+ * slots: per-run checkpoint records (36 B per run and checkpoint) for
+ * NZ_MIX_REDUCE_RECORDS, per-class sums (216 B per class and checkpoint)
+ * for NZ_MIX_REDUCE_FUSED. */
 size_t nz_mix_workspace_bytes(const NzMixSpec *spec, int32_t n_runs,
                               int32_t threads);
 /* key_dev: device pointer to the Philox key (read by the kernels, so a

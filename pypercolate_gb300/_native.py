@@ -67,7 +67,8 @@ class NzTuning(ctypes.Structure):
 class NzMixSpec(ctypes.Structure):
     _fields_ = [('grid_min', ctypes.c_uint32), ('grid_max', ctypes.c_uint32),
                 ('chain_min', ctypes.c_uint32), ('chain_max', ctypes.c_uint32),
-                ('chain_share', ctypes.c_uint32), ('checkpoints', ctypes.c_int32)]
+                ('chain_share', ctypes.c_uint32), ('checkpoints', ctypes.c_int32),
+                ('reduction', ctypes.c_int32)]
 
 
 class NzMixAccum(ctypes.Structure):

@@ -1,9 +1,11 @@
 """Autotuners for the two ensemble paths.
 
 tune_mix       batched uneven ensembles (``nz_mix``): persistent threads
-               (runs in flight), threads per CTA (runs per CTA) and the
+               (runs in flight), threads per CTA (runs per CTA), the
                shared-memory node slot per thread (placement: small lattices
-               in shared memory, the rest in HBM / L2).
+               in shared memory, the rest in HBM / L2) and the reduction
+               (per-run checkpoint records reduced by a second kernel, or
+               fused into the union-find as exact integer atomics).
 tune_ensemble  one lattice per ensemble (``nz_ensemble_tuned``): runs per
                CTA of the union-find, the probability tiles of the compensated
                m2 convolution and of the other statistics' convolution, the
@@ -46,11 +48,13 @@ def _key(spec_tuple):
 
 def tune_mix(n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5, checkpoints=256,
              sample_runs=None, cache_path=DEFAULT_CACHE, candidates=None, key=7):
-    """Best (threads, block, smem_words) for this workload and the table of
-    all timings: {'best': (...), 'table': [(threads, block, smem, G adds/s), ...]}."""
+    """Best (threads, block, smem_words, fused) for this workload and the
+    table of all timings: {'best': (...), 'table': [(threads, block, smem,
+    fused, G adds/s), ...]}.  The launch shapes are timed with the records
+    reduction; the fastest shape is then timed with the fused reduction too."""
     from .mix import MixEnsemble
     torch = nat.torch_cuda()
-    spec = (n_runs, grid[0], grid[1], chain[0], chain[1], chain_share, checkpoints)
+    spec = ('mix2', n_runs, grid[0], grid[1], chain[0], chain[1], chain_share, checkpoints)
     ck = _key(spec)
     cache = {}
     if cache_path and os.path.exists(cache_path):
@@ -65,11 +69,11 @@ def tune_mix(n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5, checkp
     nmax = max(grid[1] ** 2, chain[1])
     free, _ = torch.cuda.mem_get_info()
     cands = candidates or _candidates(nmax, free)
-    table = []
-    for threads, block, smem in cands:
+
+    def timed(threads, block, smem, fused):
         ens = MixEnsemble(sample, grid=grid, chain=chain, chain_share=chain_share,
                           checkpoints=checkpoints, threads=min(threads, sample), block=block,
-                          smem_words=smem)
+                          smem_words=smem, fused=fused)
         ens.run(key)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -79,14 +83,19 @@ def tune_mix(n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5, checkp
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        table.append((threads, block, smem, ens.additions / ms / 1e6))
+        row = (threads, block, smem, fused, ens.additions / ms / 1e6)
         del ens
         torch.cuda.empty_cache()
-    best = max(table, key=lambda t: t[3])
-    result = {'best': tuple(best[:3]), 'table': table, 'cached': False}
+        return row
+
+    table = [timed(threads, block, smem, False) for threads, block, smem in cands]
+    shape = max(table, key=lambda t: t[4])
+    table.append(timed(shape[0], shape[1], shape[2], True))
+    best = max(table, key=lambda t: t[4])
+    result = {'best': tuple(best[:4]), 'table': table, 'cached': False}
     if cache_path:
         os.makedirs(os.path.dirname(cache_path), exist_ok=True)
-        cache[ck] = {'best': list(best[:3]), 'table': table}
+        cache[ck] = {'best': list(best[:4]), 'table': table}
         with open(cache_path, 'w') as f:
             json.dump(cache, f, indent=1)
     return result

@@ -736,7 +736,8 @@ int mix_validate(const NzMixSpec *spec, int32_t n_runs, int32_t threads) {
     if (!spec || n_runs <= 0 || threads <= 0) return NZ_ERR_INVALID;
     if ((uint32_t)n_runs > NZ_MAX_RUNS) return NZ_ERR_TOO_LARGE;
     if (spec->grid_min < 1 || spec->grid_max < spec->grid_min || spec->chain_min < 1 ||
-        spec->chain_max < spec->chain_min || spec->checkpoints < 2)
+        spec->chain_max < spec->chain_min || spec->checkpoints < 2 ||
+        (spec->reduction != NZ_MIX_REDUCE_RECORDS && spec->reduction != NZ_MIX_REDUCE_FUSED))
         return NZ_ERR_INVALID;
     if ((uint64_t)spec->grid_max * spec->grid_max > NZ_MAX_NODES || spec->chain_max > NZ_MAX_NODES)
         return NZ_ERR_TOO_LARGE;
@@ -756,12 +757,19 @@ size_t mix_layout(Carver &c, const NzMixSpec &sp, int32_t n_runs, int32_t T, Mix
     L.head = c.take<uint32_t>(1);
     L.slot_off = c.take<uint64_t>((size_t)T + 1);
     L.nodes = c.take<uint32_t>((size_t)T * nmax);
-    L.rec.max_span = c.take<uint32_t>((size_t)n_runs * F);
-    L.rec.m0 = c.take<uint32_t>((size_t)n_runs * F);
-    L.rec.m2 = c.take<uint64_t>((size_t)n_runs * F);
-    L.rec.m3 = c.take<uint64_t>((size_t)n_runs * F);
-    L.rec.m4_lo = c.take<uint64_t>((size_t)n_runs * F);
-    L.rec.m4_hi = c.take<uint32_t>((size_t)n_runs * F);
+    L.fused = sp.reduction == NZ_MIX_REDUCE_FUSED;
+    L.rec = MixRec{};
+    L.cells = nullptr;
+    if (L.fused) {
+        L.cells = c.take<uint64_t>((size_t)n_classes * F * kMixCellWords);
+    } else {
+        L.rec.max_span = c.take<uint32_t>((size_t)n_runs * F);
+        L.rec.m0 = c.take<uint32_t>((size_t)n_runs * F);
+        L.rec.m2 = c.take<uint64_t>((size_t)n_runs * F);
+        L.rec.m3 = c.take<uint64_t>((size_t)n_runs * F);
+        L.rec.m4_lo = c.take<uint64_t>((size_t)n_runs * F);
+        L.rec.m4_hi = c.take<uint32_t>((size_t)n_runs * F);
+    }
     return c.used;
 }
 

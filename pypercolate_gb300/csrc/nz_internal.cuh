@@ -129,6 +129,11 @@ struct MixRec {
     uint64_t *m2, *m3, *m4_lo;
     uint32_t *m4_hi;
 };
+// Fused reduction: exact per-(class, checkpoint) sums that the union-find
+// threads accumulate themselves, kMixCellWords uint64 words per cell, each
+// the sum of one 32-bit limb of a statistic (or of its square) over the
+// class's runs.
+constexpr int kMixCellWords = 27;
 struct MixAccum {
     uint32_t *count;
     uint32_t *span;
@@ -144,7 +149,9 @@ struct MixLaunch {
     uint32_t *nodes;
     int32_t T, block;
     uint32_t smem_words;
-    MixRec rec;
+    bool fused;       // NZ_MIX_REDUCE_FUSED: cells, else records + mix_reduce_kernel
+    MixRec rec;       // [n_runs][F] per plane (records only)
+    uint64_t *cells;  // [classes][F][kMixCellWords] (fused only)
     MixAccum acc;
 };
 int launch_mix(const MixLaunch &p, cudaStream_t s);

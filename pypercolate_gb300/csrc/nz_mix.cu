@@ -19,11 +19,17 @@
 //      first (its node slot is sized for it), then claims further items with
 //      an atomic counter; S only decreases along the queue, so every later
 //      item fits the slot.  Small items (S words <= smem slot) run in shared
-//      memory.  Each run writes its exact statistics at F evenly spaced
-//      occupation checkpoints n_j = floor(j M / (F - 1)).
+//      memory.  At F evenly spaced occupation checkpoints
+//      n_j = floor(j M / (F - 1)) each run either writes its exact
+//      statistics (records) or, with the fused reduction, adds them and
+//      their squares into its class's cell j itself (integer atomics of
+//      32-bit limbs: exact, and independent of the order the runs finish in);
 //   6. mix_reduce_kernel  : per (class, checkpoint) exact integer sums of x
-//      and x^2 (up to 192 bits) over the runs of the class -> mean and M2
-//      (percolate/percolate.py:450-705 semantics at those n).
+//      and x^2 (up to 192 bits) over the class's records -> mean and M2
+//      (percolate/percolate.py:450-705 semantics at those n); or
+//      mix_finalize_kernel: the same sums and M2 from the fused cells.
+//   Both reductions give identical results; which is faster depends on the
+//   mix of lattices (many runs per lattice favour the fused one).
 #include <cmath>
 #include <cstdint>
 
@@ -178,10 +184,104 @@ __device__ __forceinline__ void add128m(uint64_t &lo, uint64_t &hi, uint64_t blo
     lo = nlo;
 }
 
-// One complete run in `node` (global or shared), writing its checkpoints.
-template <int KIND>
+// ------------------------------------------------------- fused reduction
+// Cell words.  Each word sums one 32-bit limb over the class's runs: at most
+// NZ_MAX_RUNS = 2^24 limbs < 2^32, so no word can overflow.  With N <= 2^21:
+// max, m0 < 2^21, m2 < 2^42, m3 < 2^63, m4 < 2^84.
+//   0 runs with a spanning cluster
+//   sums of x:   1 max, 2 m0, 3-4 m2, 5-6 m3, 7-9 m4
+//   sums of x^2: 10-11 max, 12-13 m0, 14-16 m2, 17-20 m3, 21-26 m4
+// (m1 = N - max follows from the max sums.)
+constexpr int kCellSpan = 0, kSxMax = 1, kSxM0 = 2, kSxM2 = 3, kSxM3 = 5, kSxM4 = 7;
+constexpr int kSqMax = 10, kSqM0 = 12, kSqM2 = 14, kSqM3 = 17, kSqM4 = 21;
+static_assert(kSqM4 + 6 == kMixCellWords, "cell layout");
+
+// Adds 32-bit limbs into the words of one cell.  When every active lane of
+// the warp adds into the same cell (runs of one lattice reach their
+// checkpoints together), the lanes' limbs are summed first (redux.sync on
+// 16-bit halves, so 32 lanes' sums fit 32 bits) and one lane issues the
+// atomic: 27 atomics per warp and checkpoint instead of up to 27 x 32.
+struct CellAdder {
+    uint64_t *cell;
+    unsigned mask;
+    bool warp, leader;
+    __device__ __forceinline__ explicit CellAdder(uint64_t *c) : cell(c) {
+        mask = __activemask();
+        warp = __match_any_sync(mask, (unsigned long long)(uintptr_t)c) == mask;
+        leader = (threadIdx.x & 31u) == (unsigned)(__ffs(mask) - 1);
+    }
+    __device__ __forceinline__ void limb(int k, uint32_t v) const {
+        if (warp) {
+            const uint32_t lo = __reduce_add_sync(mask, v & 0xffffu);
+            const uint32_t hi = __reduce_add_sync(mask, v >> 16);
+            const uint64_t sum = (uint64_t)lo + ((uint64_t)hi << 16);
+            if (leader && sum) atomicAdd(reinterpret_cast<unsigned long long *>(cell + k), (unsigned long long)sum);
+        } else if (v) {
+            atomicAdd(reinterpret_cast<unsigned long long *>(cell + k), (unsigned long long)v);
+        }
+    }
+    __device__ __forceinline__ void u64(int k, uint64_t v) const {
+        limb(k, (uint32_t)v);
+        limb(k + 1, (uint32_t)(v >> 32));
+    }
+    template <int LIMBS>
+    __device__ __forceinline__ void wide(int k, u128 v) const {
+#pragma unroll
+        for (int i = 0; i < LIMBS; ++i) limb(k + i, (uint32_t)(v >> (32 * i)));
+    }
+};
+
+// One run's statistics at one checkpoint into its class's cell.
+__device__ __forceinline__ void mix_checkpoint(uint64_t *cell, uint32_t mx, bool span, uint32_t m0, uint64_t m2,
+                                               uint64_t m3, uint64_t m4lo, uint32_t m4hi) {
+    const CellAdder a(cell);
+    a.limb(kCellSpan, span ? 1u : 0u);
+    a.limb(kSxMax, mx);
+    a.limb(kSxM0, m0);
+    a.u64(kSxM2, m2);
+    a.u64(kSxM3, m3);
+    a.u64(kSxM4, m4lo);
+    a.limb(kSxM4 + 2, m4hi);
+    a.u64(kSqMax, (uint64_t)mx * mx);
+    a.u64(kSqM0, (uint64_t)m0 * m0);
+    a.wide<3>(kSqM2, (u128)m2 * m2);
+    a.wide<4>(kSqM3, (u128)m3 * m3);
+    // m4^2 = lo^2 + 2 lo hi 2^64 + hi^2 2^128 (< 2^168) as three 64-bit words
+    const u128 ll = (u128)m4lo * m4lo;
+    const u128 mid = ((u128)m4lo * m4hi) << 1;  // < 2^85
+    const u128 t = (ll >> 64) + (uint64_t)mid;  // < 2^65
+    a.u64(kSqM4, (uint64_t)ll);
+    a.u64(kSqM4 + 2, (uint64_t)t);
+    a.u64(kSqM4 + 4, (uint64_t)(t >> 64) + (uint64_t)(mid >> 64) + (uint64_t)m4hi * m4hi);
+}
+
+// Where a run's checkpoints go: its records (queue position `pos`, F
+// entries) or its class's F cells.
+template <bool FUSED>
+struct MixSink {
+    MixRec rec;
+    size_t rec_base;
+    uint64_t *cells;
+    __device__ __forceinline__ void put(uint32_t j, uint32_t mx, bool span, uint32_t m0, uint64_t m2, uint64_t m3,
+                                        uint64_t m4lo, uint32_t m4hi) const {
+        if (FUSED) {
+            mix_checkpoint(cells + (size_t)j * kMixCellWords, mx, span, m0, m2, m3, m4lo, m4hi);
+        } else {
+            const size_t off = rec_base + j;
+            rec.max_span[off] = mx | (span ? kSpanBit : 0u);
+            rec.m0[off] = m0;
+            rec.m2[off] = m2;
+            rec.m3[off] = m3;
+            rec.m4_lo[off] = m4lo;
+            rec.m4_hi[off] = m4hi;
+        }
+    }
+};
+
+// One complete run in `node` (global or shared), delivering its checkpoints.
+template <int KIND, bool FUSED>
 __device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L, uint32_t N, uint32_t M, uint32_t *node,
-                        const MixRec &out, size_t rec_base) {
+                        const MixSink<FUSED> &out) {
     GraphDev g;
     g.kind = KIND; g.site = 0; g.wrap = 0; g.L = L; g.N = N; g.M = M;
     g.tile_cols = KIND == NZ_GRAPH_GRID2D ? (L + 3u) >> 2 : 0u;  // grids in the tiled layout
@@ -245,24 +345,26 @@ __device__ void mix_run(const MixDev &m, uint64_t key, uint32_t run, uint32_t L,
                 if (sides == 3u) span = true;
             }
         }
-        while (j < (uint32_t)m.F && n == target) {
-            const size_t off = rec_base + j;
-            out.max_span[off] = mx | (span ? kSpanBit : 0u);
-            out.m0[off] = t0 - 1u;
-            out.m2[off] = t2 - mx2;
-            out.m3[off] = t3 - mx3;
-            out.m4_lo[off] = t4lo - mx4lo;
-            out.m4_hi[off] = (uint32_t)(t4hi - mx4hi - (t4lo < mx4lo ? 1ull : 0ull));
-            ++j;
-            if (j < (uint32_t)m.F) target = next_row(j);
+        if (n == target) {
+            const uint64_t m4lo = t4lo - mx4lo;
+            const uint32_t m4hi = (uint32_t)(t4hi - mx4hi - (t4lo < mx4lo ? 1ull : 0ull));
+            // several checkpoints share row n when F - 1 > M
+            while (j < (uint32_t)m.F && n == target) {
+                out.put(j, mx, span, t0 - 1u, t2 - mx2, t3 - mx3, m4lo, m4hi);
+                ++j;
+                if (j < (uint32_t)m.F) target = next_row(j);
+            }
         }
     }
 }
 
-__global__ void __launch_bounds__(256) mix_uf_kernel(MixDev m, const uint32_t *queue, const uint32_t *cls,
-                                                     int32_t T, const uint64_t *slot_off, uint32_t *nodes,
-                                                     uint32_t smem_words, uint32_t *head, MixRec out,
-                                                     uint32_t *errors) {
+// (256, 3): at most 85 registers (80 used by either reduction), so that 6
+// CTAs of 128 threads stay resident per SM
+template <bool FUSED>
+__global__ void __launch_bounds__(256, 3) mix_uf_kernel(MixDev m, const uint32_t *queue, const uint32_t *cls,
+                                                        int32_t T, const uint64_t *slot_off, uint32_t *nodes,
+                                                        uint32_t smem_words, uint32_t *head, MixRec rec,
+                                                        uint64_t *cells, uint32_t *errors) {
     extern __shared__ uint32_t s_nodes[];
     const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T || t >= m.n_runs) return;
@@ -282,9 +384,12 @@ __global__ void __launch_bounds__(256) mix_uf_kernel(MixDev m, const uint32_t *q
             pos = atomicAdd(head, 1u);
             continue;
         }
-        const size_t base = (size_t)pos * (uint32_t)m.F;
-        if (kind == NZ_GRAPH_GRID2D) mix_run<NZ_GRAPH_GRID2D>(m, key, run, L, N, M, node, out, base);
-        else mix_run<NZ_GRAPH_CHAIN1D>(m, key, run, L, N, M, node, out, base);
+        MixSink<FUSED> out;
+        out.rec = rec;
+        out.rec_base = (size_t)pos * (uint32_t)m.F;
+        out.cells = cells + (size_t)cls[run] * (uint32_t)m.F * kMixCellWords;
+        if (kind == NZ_GRAPH_GRID2D) mix_run<NZ_GRAPH_GRID2D, FUSED>(m, key, run, L, N, M, node, out);
+        else mix_run<NZ_GRAPH_CHAIN1D, FUSED>(m, key, run, L, N, M, node, out);
         pos = atomicAdd(head, 1u);
     }
 }
@@ -397,6 +502,66 @@ __global__ void mix_reduce_kernel(MixDev m, const uint32_t *counts, const uint32
     }
 }
 
+// a + (w << (32 k)) for a cell word w < 2^64
+__device__ __forceinline__ void u256_add_limb(U256 &a, uint64_t w, int k) {
+    U256 t = {{0, 0, 0, 0}};
+    const int q = k >> 1;
+    if (k & 1) {
+        t.w[q] = w << 32;
+        if (q + 1 < 4) t.w[q + 1] = w >> 32;
+    } else {
+        t.w[q] = w;
+    }
+    u256_add(a, t);
+}
+__device__ __forceinline__ U256 cell_sum(const uint64_t *w, int limbs) {
+    U256 r = {{0, 0, 0, 0}};
+    for (int k = 0; k < limbs; ++k) u256_add_limb(r, w[k], k);
+    return r;
+}
+
+// thread = cell (class c, checkpoint j): the fused limb sums -> exact sums
+// of x and M2 = (cnt * sum x^2 - (sum x)^2) / cnt from the exact 256-bit
+// numerator, as mix_reduce_kernel computes them from the records.
+__global__ void mix_finalize_kernel(MixDev m, const uint32_t *counts, const uint64_t *cells, MixAccum acc,
+                                    uint32_t n_classes) {
+    const size_t plane = (size_t)n_classes * (uint32_t)m.F;
+    const size_t cj = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (cj >= plane) return;
+    const uint32_t c = (uint32_t)(cj / (uint32_t)m.F), j = (uint32_t)(cj % (uint32_t)m.F);
+    const uint32_t cnt = counts[c];
+    uint32_t kind, L, N, M;
+    class_graph(m, c, kind, L, N, M);
+    (void)kind; (void)L; (void)M;
+    const uint64_t *w = cells + cj * kMixCellWords;
+    const u128 sx_max = cell_sum(w + kSxMax, 1).w[0];
+    const U256 sq_max = cell_sum(w + kSqMax, 2);
+    // m1 = N - max: sum (N - x) = cnt N - sum x; sum (N - x)^2 = cnt N^2 - 2 N sum x + sum x^2 (< 2^67)
+    const u128 sq_max128 = ((u128)sq_max.w[1] << 64) | sq_max.w[0];
+    const u128 sx_m1 = (u128)cnt * N - sx_max;
+    const u128 sq_m1 = (u128)cnt * N * N + sq_max128 - (u128)(2ull * N) * sx_max;
+    U256 sx[6], sq[6];
+    sx[0] = cell_sum(w + kSxMax, 1);  sq[0] = sq_max;
+    sx[1] = cell_sum(w + kSxM0, 1);   sq[1] = cell_sum(w + kSqM0, 2);
+    sx[2] = u256_from_u128(sx_m1);    sq[2] = u256_from_u128(sq_m1);
+    sx[3] = cell_sum(w + kSxM2, 2);   sq[3] = cell_sum(w + kSqM2, 3);
+    sx[4] = cell_sum(w + kSxM3, 2);   sq[4] = cell_sum(w + kSqM3, 4);
+    sx[5] = cell_sum(w + kSxM4, 3);   sq[5] = cell_sum(w + kSqM4, 6);
+    if (j == 0) acc.count[c] = cnt;
+    acc.span[cj] = (uint32_t)w[kCellSpan];
+    for (int k = 0; k < 6; ++k) {
+        const u128 sum = ((u128)sx[k].w[1] << 64) | sx[k].w[0];  // < 2^108
+        acc.sum_lo[k * plane + cj] = (uint64_t)sum;
+        acc.sum_hi[k * plane + cj] = (uint64_t)(sum >> 64);
+        double m2 = 0.0;
+        if (cnt > 0) {
+            const U256 num = u256_sub(u256_mul64(sq[k], cnt), u128_sq(sum));
+            m2 = u256_to_f64(num) / (double)cnt;
+        }
+        acc.m2[k * plane + cj] = m2;
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 int launch_mix(const MixLaunch &p, cudaStream_t s) {
@@ -413,14 +578,29 @@ int launch_mix(const MixLaunch &p, cudaStream_t s) {
     const uint32_t first_free = (uint32_t)(p.T < p.m.n_runs ? p.T : p.m.n_runs);
     mix_head_kernel<<<1, 1, 0, s>>>(p.head, first_free);
     const size_t smem = (size_t)p.smem_words * 4u * (size_t)p.block;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(mix_uf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return NZ_ERR_INVALID;
-    mix_uf_kernel<<<(p.T + p.block - 1) / p.block, p.block, smem, s>>>(p.m, p.queue, p.cls, p.T, p.slot_off,
-                                                                        p.nodes, p.smem_words, p.head, p.rec,
-                                                                        p.acc.errors);
-    dim3 rg(n_classes, (p.m.F + 31) / 32);
-    mix_reduce_kernel<<<rg, 32, 0, s>>>(p.m, p.counts, p.offsets, p.rec, p.acc, n_classes);
+    const unsigned grid = (unsigned)((p.T + p.block - 1) / p.block);
+    if (p.fused) {
+        const size_t cells = (size_t)n_classes * (uint32_t)p.m.F;
+        if (cudaMemsetAsync(p.cells, 0, cells * kMixCellWords * sizeof(uint64_t), s) != cudaSuccess)
+            return NZ_ERR_CUDA;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(mix_uf_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+            return NZ_ERR_INVALID;
+        mix_uf_kernel<true><<<grid, p.block, smem, s>>>(p.m, p.queue, p.cls, p.T, p.slot_off, p.nodes, p.smem_words,
+                                                        p.head, p.rec, p.cells, p.acc.errors);
+        mix_finalize_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(p.m, p.counts, p.cells, p.acc,
+                                                                            n_classes);
+    } else {
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(mix_uf_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+            return NZ_ERR_INVALID;
+        mix_uf_kernel<false><<<grid, p.block, smem, s>>>(p.m, p.queue, p.cls, p.T, p.slot_off, p.nodes,
+                                                         p.smem_words, p.head, p.rec, p.cells, p.acc.errors);
+        dim3 rg(n_classes, (p.m.F + 31) / 32);
+        mix_reduce_kernel<<<rg, 32, 0, s>>>(p.m, p.counts, p.offsets, p.rec, p.acc, n_classes);
+    }
     return cudaGetLastError() == cudaSuccess ? NZ_OK : NZ_ERR_CUDA;
 }
 

@@ -8,6 +8,11 @@ log-uniform in its range and rounded to the nearest integer
 ``checkpoints`` evenly spaced occupation numbers to exact sums and M2 of the
 microcanonical statistics (percolate/percolate.py:450-705 at those n).
 
+``fused=True`` reduces the runs inside the persistent union-find (each run
+adds its statistics and their squares into its lattice's exact sums by
+integer atomics) instead of writing per-run checkpoint records for a second
+kernel; the results are identical.
+
 ``MixEnsemble.capture()`` records the whole launch sequence in a CUDA graph;
 ``replay(key)`` re-runs it for another key without re-launching from Python.
 """
@@ -38,7 +43,7 @@ class MixEnsemble:
     """One batched uneven ensemble configuration (sizes fixed, key varies)."""
 
     def __init__(self, n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5,
-                 checkpoints=256, threads=None, block=128, smem_words=0):
+                 checkpoints=256, threads=None, block=128, smem_words=0, fused=False):
         torch = nat.torch_cuda()
         self.n_runs = int(n_runs)
         self.spec = nat.NzMixSpec()
@@ -46,6 +51,8 @@ class MixEnsemble:
         self.spec.chain_min, self.spec.chain_max = int(chain[0]), int(chain[1])
         self.spec.chain_share = min(int(round(chain_share * 2 ** 32)), 2 ** 32 - 1)
         self.spec.checkpoints = int(checkpoints)
+        self.spec.reduction = 1 if fused else 0
+        self.fused = bool(fused)
         self.F = int(checkpoints)
         self.n_grid = grid[1] - grid[0] + 1
         self.n_chain = chain[1] - chain[0] + 1

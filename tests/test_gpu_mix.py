@@ -53,12 +53,12 @@ def _oracle_mix(oracle, ens, key):
     return count, span, sums, sq
 
 
-@pytest.mark.parametrize('smem_words', [0, 128])
-def test_mix_exact_against_oracle(gpu, oracle, smem_words):
+@pytest.mark.parametrize('smem_words,fused', [(0, False), (128, False), (0, True), (128, True)])
+def test_mix_exact_against_oracle(gpu, oracle, smem_words, fused):
     from pypercolate_gb300.mix import MixEnsemble
     key = 0x1234567890
     ens = MixEnsemble(1500, grid=(3, 20), chain=(10, 300), chain_share=0.5, checkpoints=16,
-                      threads=256, block=64, smem_words=smem_words)
+                      threads=256, block=64, smem_words=smem_words, fused=fused)
     ens.run(key)
     got = ens.results()
     count, span, sums, sq = _oracle_mix(oracle, ens, key)
@@ -89,3 +89,43 @@ def test_mix_graph_replay(gpu):
         assert np.array_equal(ga[k], gb[k]), k
     a.replay(78)
     assert not np.array_equal(a.results()['sum_lo'], gb['sum_lo'])
+
+
+def test_mix_fused_equals_records(gpu):
+    """The reduction fused into the union-find (integer atomics into per-lattice
+    sums) gives the same integers and M2 as per-run records reduced by a
+    second kernel, including lattices with more checkpoints than rows
+    (F - 1 > M: several checkpoints per row) and runs sharing warps."""
+    from pypercolate_gb300.mix import MixEnsemble
+    out = []
+    for fused in (False, True):
+        e = MixEnsemble(20000, grid=(2, 64), chain=(3, 5000), chain_share=0.4, checkpoints=300,
+                        threads=4096, block=128, fused=fused)
+        e.run(99)
+        out.append(e.results())
+    for k in out[0]:
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_mix_fused_graph_replay(gpu):
+    from pypercolate_gb300.mix import MixEnsemble
+    a = MixEnsemble(3000, grid=(4, 40), chain=(50, 2000), chain_share=0.3, checkpoints=8,
+                    threads=512, block=128, fused=True)
+    a.capture()
+    a.replay(77)
+    ga = a.results()
+    b = MixEnsemble(3000, grid=(4, 40), chain=(50, 2000), chain_share=0.3, checkpoints=8,
+                    threads=512, block=128, fused=False)
+    b.run(77)
+    gb = b.results()
+    for k in ga:
+        assert np.array_equal(ga[k], gb[k]), k
+
+
+def test_tune_mix_times_both_reductions(gpu):
+    from pypercolate_gb300.autotune import tune_mix
+    t = tune_mix(4000, grid=(4, 24), chain=(64, 1024), checkpoints=32, cache_path=None,
+                 candidates=[(1024, 128, 0), (2048, 64, 0)])
+    assert len(t['best']) == 4
+    assert [row[3] for row in t['table']] == [False, False, True]
+    assert all(row[4] > 0 for row in t['table'])

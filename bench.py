@@ -169,6 +169,12 @@ def parse():
     ap.add_argument('--plain-runs', type=int, default=8192,
                     help='runs timed on the plain path (0: skip)')
     ap.add_argument('--plain-chunk', type=int, default=4096)
+    ap.add_argument('--surrogate-weights', default='se', choices=['none', 'se'],
+                    help='surrogate study: weight the training loss by the Monte Carlo '
+                         'standard errors of the targets')
+    ap.add_argument('--surrogate-se-floor', type=float, default=0.01,
+                    help='surrogate study: standardised error added to each target\'s '
+                         'standard error in its loss weight')
     ap.add_argument('--surrogate-steps', type=int, default=30000,
                     help='Adam steps of --study surrogate')
     ap.add_argument('--no-tune', dest='tune', action='store_false',
@@ -413,21 +419,24 @@ def surrogate_study(args):
     lattices = [('grid', L) for L in (16, 24, 32, 48, 64, 96, 128, 192, 256, 320, 448, 512)] + \
                [('chain', l) for l in (1024, 2048, 4096, 8192, 16384, 32768, 65536)]
     t0 = time.perf_counter()
-    X, Y = [], []
+    X, Y, SE = [], [], []
     for kind, L in lattices:
         M = 2 * L * (L - 1) if kind == 'grid' else L - 1
         runs = int(min(20000, max(1000, 2e9 / M)))
         grid = S.training_grid(kind, L, P)
-        y, _ = S.ensemble_targets(kind, L, grid, runs, key=L)
+        y, s = S.ensemble_targets(kind, L, grid, runs, key=L)
         X.append(S.features(grid, L, kind))
         Y.append(S.train_targets(y))
-    X, Y = np.concatenate(X), np.concatenate(Y)
+        SE.append(S.train_se(y, s))
+    X, Y, SE = np.concatenate(X), np.concatenate(Y), np.concatenate(SE)
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     model = S.MLP(seed=0)
     steps, batch = args.surrogate_steps, 4096
     t0 = time.perf_counter()
-    trace = model.fit(X, Y, steps=steps, batch=batch, lr=1e-3, log_every=1000, decay=0.05)
+    weighted = args.surrogate_weights == 'se'
+    trace = model.fit(X, Y, steps=steps, batch=batch, lr=1e-3, log_every=1000, decay=0.05,
+                      se=SE if weighted else None, se_floor=args.surrogate_se_floor)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     dense = np.linspace(0.0, 1.0, 2001)
@@ -456,6 +465,8 @@ def surrogate_study(args):
             'lattices': ['%s %d' % t for t in lattices], 'p_per_lattice': P,
             'p_grid': 'half uniform, half in the finite-size transition window',
             'data_seconds': t_data, 'train_seconds': t_train, 'steps': steps, 'batch': batch,
+            'loss_weights': ('1 / (se^2 + %g^2), standardised Monte Carlo standard errors'
+                             % args.surrogate_se_floor if weighted else 'none'),
             'samples_per_s': steps * batch / t_train, 'loss_trace': trace,
             'held_out': 'square L=384, 8000 runs, 2001 p',
             'accepted_fraction_2se': acc, 'p_grid_gain_spanning': gains,

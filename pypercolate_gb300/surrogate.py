@@ -97,6 +97,14 @@ def train_targets(y):
     return out
 
 
+def train_se(y, se):
+    """Standard errors of the curves (``ensemble_targets``) in the units the
+    network learns (``train_targets``): the strength's error relative."""
+    out = np.array(se, dtype=np.float64, copy=True)
+    out[:, 1] = out[:, 1] / np.maximum(np.asarray(y)[:, 1], STRENGTH_FLOOR)
+    return out
+
+
 def curves(pred):
     """Network outputs back to (spanning probability, strength, log
     susceptibility)."""
@@ -196,10 +204,15 @@ class MLP:
         nat.check(nat.lib_handle().nz_mlp_take_errors(ctypes.byref(v)), 'nz_mlp_take_errors')
         return int(v.value)
 
-    def fit(self, X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, log_every=0, decay=0.0):
+    def fit(self, X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, log_every=0, decay=0.0,
+            se=None, se_floor=0.01):
         """Standardise, then Adam on random mini-batches; the learning rate
         stays `lr`, then (decay > 0) falls geometrically to lr * decay over
-        the last third of the steps.  Returns the loss trace."""
+        the last third of the steps.  With `se` (the targets' Monte Carlo
+        standard errors, same shape and units as Y) the squared errors are
+        weighted by 1 / (se^2 + se_floor^2) in standardised units, normalised
+        to mean 1 per output: precisely known points count more, points the
+        ensembles hardly determine less.  Returns the loss trace."""
         torch = nat.torch_cuda()
         X = np.asarray(X, np.float32)
         Y = np.asarray(Y, np.float32)
@@ -207,6 +220,12 @@ class MLP:
         self.y_mean, self.y_std = Y.mean(0), Y.std(0) + 1e-6
         dX = torch.from_numpy((X - self.x_mean) / self.x_std).cuda()
         dY = torch.from_numpy((Y - self.y_mean) / self.y_std).cuda()
+        dW = None
+        if se is not None:
+            s = np.asarray(se, np.float64) / self.y_std
+            w = 1.0 / (s * s + se_floor * se_floor)
+            w /= w.mean(0)
+            dW = torch.from_numpy(w.astype(np.float32)).cuda()
         gen = torch.Generator(device='cuda')
         gen.manual_seed(seed)
         n = dX.shape[0]
@@ -214,7 +233,8 @@ class MLP:
         trace = []
         for k in range(steps):
             idx = torch.randint(0, n, (batch,), device='cuda', generator=gen)
-            loss = self.loss_and_grads(dX[idx].contiguous(), dY[idx].contiguous())
+            loss = self.loss_and_grads(dX[idx].contiguous(), dY[idx].contiguous(),
+                                       None if dW is None else dW[idx].contiguous())
             rate = lr
             if decay > 0.0 and k > 2 * steps // 3:
                 rate = lr * decay ** ((k - 2 * steps // 3) / max(1, steps - 2 * steps // 3))

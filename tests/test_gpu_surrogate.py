@@ -73,6 +73,26 @@ def test_training_fits_a_smooth_function(gpu):
     assert np.sqrt(np.mean((pred - Y[:2000]) ** 2)) < 0.1
 
 
+def test_standard_error_weights(gpu):
+    """Loss weights 1 / (se^2 + floor^2), normalised to mean 1: equal errors
+    reproduce the unweighted training exactly; a half of the rows with small
+    errors is then fitted better than without weights."""
+    from pypercolate_gb300.surrogate import MLP
+    rng = np.random.default_rng(3)
+    X = rng.uniform(0, 1, size=(8192, 5)).astype(np.float32)
+    Y = np.column_stack([np.sin(6 * X[:, 0]) * X[:, 1], np.cos(5 * X[:, 2]), X[:, 3] * X[:, 4]])
+    a = MLP(seed=4).fit(X, Y, steps=200, batch=4096, log_every=50)
+    b = MLP(seed=4).fit(X, Y, steps=200, batch=4096, log_every=50, se=np.full(Y.shape, 0.2))
+    assert a == b
+    precise = X[:, 0] < 0.5
+    se = np.where(precise[:, None], 1e-3, 1.0) * np.ones_like(Y)
+    plain, weighted = MLP(seed=5), MLP(seed=5)
+    plain.fit(X, Y, steps=600, batch=4096)
+    weighted.fit(X, Y, steps=600, batch=4096, se=se)
+    err = lambda m: np.sqrt(np.mean((m.predict(X[precise]) - Y[precise]) ** 2))  # noqa: E731
+    assert err(weighted) < err(plain)
+
+
 def test_surrogate_pipeline_small(gpu):
     """Train on square lattices L in {8..48} minus 28, judge at L=28 by Monte
     Carlo, and check that surrogate-placed p-grids interpolate the held-out

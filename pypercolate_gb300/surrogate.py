@@ -6,8 +6,9 @@ asinh((p - p_c) L^(1/nu)) derived from them (p_c = 1/2, nu = 4/3 for bond
 percolation on the square lattice; p_c = 1, nu = 1 for the chain), on which
 the curves of different L collapse -- to (spanning probability, percolation
 strength, log-susceptibility), where susceptibility = m2 / N (the mean size
-of the non-largest clusters, sum' s^2 / N); the strength is learned as its
-logarithm (``train_targets``, ``curves``).  It is trained with the library's
+of the non-largest clusters, sum' s^2 / N); the spanning probability is
+learned as its logit and the strength as its logarithm (``train_targets``,
+``curves``).  It is trained with the library's
 own forward, backward and Adam kernels (libnzgb300 ``nz_mlp_*``: tcgen05
 GEMMs with BF16 operands and FP32 accumulation) on ensembles that this
 package's GPU path generates.
@@ -85,23 +86,34 @@ def ensemble_targets(kind, L, ps, runs, key=11, run0=0, precision='fp32'):
 
 
 STRENGTH_FLOOR = 1e-12
+SPAN_EPS = 1e-6
 
 
 def train_targets(y):
-    """The curves as the network learns them: spanning probability as is,
-    log strength and log susceptibility.  Below the threshold the strength
-    is ~log(N)/N and its Monte Carlo error ~1e-6: in log units the network's
-    error is relative, so it can come within the judge's error bars there."""
+    """The curves as the network learns them: the logit of the spanning
+    probability (clipped to [1e-6, 1 - 1e-6]), log strength and log
+    susceptibility.  Away from the threshold the spanning probability is 0
+    or 1 to within its Monte Carlo error (~1/runs), and below it the
+    strength is ~log(N)/N with an error ~1e-6: in logit and log units the
+    network's error is relative there, so it can come within the judge's
+    error bars."""
     out = np.array(y, dtype=np.float64, copy=True)
+    pi = np.clip(out[:, 0], SPAN_EPS, 1.0 - SPAN_EPS)
+    out[:, 0] = np.log(pi) - np.log1p(-pi)
     out[:, 1] = np.log(np.maximum(out[:, 1], STRENGTH_FLOOR))
     return out
 
 
 def train_se(y, se):
     """Standard errors of the curves (``ensemble_targets``) in the units the
-    network learns (``train_targets``): the strength's error relative."""
+    network learns (``train_targets``), to first order: the spanning error
+    divided by pi (1 - pi) (at most one logit unit where pi is within its
+    error of 0 or 1), the strength's error relative."""
+    y = np.asarray(y, dtype=np.float64)
     out = np.array(se, dtype=np.float64, copy=True)
-    out[:, 1] = out[:, 1] / np.maximum(np.asarray(y)[:, 1], STRENGTH_FLOOR)
+    pi = y[:, 0]
+    out[:, 0] = out[:, 0] / np.maximum(pi * (1.0 - pi), out[:, 0])
+    out[:, 1] = out[:, 1] / np.maximum(y[:, 1], STRENGTH_FLOOR)
     return out
 
 
@@ -109,6 +121,7 @@ def curves(pred):
     """Network outputs back to (spanning probability, strength, log
     susceptibility)."""
     out = np.array(pred, dtype=np.float64, copy=True)
+    out[:, 0] = 0.5 * (1.0 + np.tanh(0.5 * out[:, 0]))  # the logistic function, overflow-free
     out[:, 1] = np.exp(out[:, 1])
     return out
 

@@ -278,8 +278,11 @@ int nz_microcanonical_finalize(const NzMicroAccum *acc, uint32_t num_nodes,
                                uint32_t num_edges, int32_t spanning,
                                double alpha, int32_t normalize, double *out,
                                void *stream);
-/* (normalize = 0: absolute units as microcanonical_averages yields them,
- * percolate/percolate.py:708-896; 1: divided by N as in the arrays.) */
+/* (normalize bit 0 = 0: absolute units as microcanonical_averages yields
+ * them, percolate/percolate.py:708-896; 1: divided by N as in the arrays.
+ * With NZ_MICRO_FIELD_MAJOR or-ed in, out is field-major instead:
+ * out[j * (M + 1) + n], each value's M + 1 rows contiguous.) */
+#define NZ_MICRO_FIELD_MAJOR 2
 
 /* Adds the runs of a record set (rows n_begin..n_end-1 of all its runs; the
  * records' row 0 is n_begin) to the accumulators: the run-reductions of

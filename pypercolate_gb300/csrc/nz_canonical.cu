@@ -1363,24 +1363,35 @@ void launch_finalize(const uint8_t *avg, int32_t P, int32_t spanning, double N, 
 // std/sqrt(R), std with ddof 1, (mean, mean) where std == 0; max and moments
 // divided by N as microcanonical_averages_arrays returns them.
 // out[n * 21 + ...]: span (mean, lo, hi), max (mean, lo, hi), m0..m4 (mean, lo, hi).
+// Two threads per row n: half 0 the spanning mean, the lower Beta bound and
+// statistics max, m0, m1; half 1 the upper Beta bound and m2, m3, m4 -- the
+// Beta quantiles (iterative, FP64) are most of the work, and rows where some
+// but not all runs span are contiguous, so splitting them doubles the
+// threads working on those rows.
 __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
                                       int32_t normalize, double *out) {
-    const uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = t >> 1, half = t & 1u;
     const double R = (double)*acc.count;
     // every row has R runs: one pair of t quantiles per block
     const TPair tq = t_pair_block(1.0 - alpha, R - 1.0, R - 1.0, n <= M);
     if (n > M) return;
-    double *o = out + (size_t)n * 21;
+    // value j of row n: out[n * 21 + j], or out[j * (M + 1) + n] field-major
+    const bool fields = (normalize & NZ_MICRO_FIELD_MAJOR) != 0;
+    auto put = [&](int j, double v) { out[fields ? (size_t)j * (M + 1) + n : (size_t)n * 21 + j] = v; };
     if (spanning) {
         const double k = (double)acc.span_count[n];
-        o[0] = (k + 1.0) / (R + 2.0);
-        o[1] = beta_quantile(alpha / 2.0, k + 1.0, R - k + 1.0);
-        o[2] = beta_quantile(1.0 - alpha / 2.0, k + 1.0, R - k + 1.0);
-    } else {
-        o[0] = o[1] = o[2] = NAN;
+        if (half == 0) {
+            put(0, (k + 1.0) / (R + 2.0));
+            put(1, beta_quantile(alpha / 2.0, k + 1.0, R - k + 1.0));
+        } else {
+            put(2, beta_quantile(1.0 - alpha / 2.0, k + 1.0, R - k + 1.0));
+        }
+    } else if (half == 0) {
+        put(0, NAN); put(1, NAN); put(2, NAN);
     }
     const int map[6] = {0, 1, 2, 3, 4, 5};  // max, m0, m1, m2, m3, m4
-    for (int j = 0; j < 6; ++j) {
+    for (int j = 3 * (int)half; j < 3 * (int)half + 3; ++j) {
         const size_t idx = (size_t)map[j] * (M + 1) + n;
         const double mean = fma((double)acc.sum_hi[idx], 18446744073709551616.0, (double)acc.sum_lo[idx]) / R;
         const double m2 = acc.m2[idx];
@@ -1391,16 +1402,18 @@ __global__ void micro_finalize_kernel(NzMicroAccum acc, uint32_t N, uint32_t M, 
             lo = mean + sc * tq.lo;
             hi = mean + sc * tq.hi;
         }
-        const double scale = normalize ? (double)N : 1.0;
-        o[3 + 3 * j] = mean / scale;
-        o[4 + 3 * j] = lo / scale;
-        o[5 + 3 * j] = hi / scale;
+        const double scale = (normalize & 1) ? (double)N : 1.0;
+        put(3 + 3 * j, mean / scale);
+        put(4 + 3 * j, lo / scale);
+        put(5 + 3 * j, hi / scale);
     }
 }
 
 void launch_micro_finalize(const NzMicroAccum &acc, uint32_t N, uint32_t M, int32_t spanning, double alpha,
                            int32_t normalize, double *out, cudaStream_t s) {
-    micro_finalize_kernel<<<(M + 1 + 127) / 128, 128, 0, s>>>(acc, N, M, spanning, alpha, normalize, out);
+    const uint64_t threads = 2ull * ((uint64_t)M + 1);
+    micro_finalize_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, s>>>(acc, N, M, spanning, alpha, normalize,
+                                                                          out);
 }
 
 __global__ void t_quantile_kernel(const double *q, const double *df, int32_t count, double *out) {

@@ -12,6 +12,8 @@
 //     falling back to bisection whenever a Newton step leaves the bracket.
 //     The t start value is the Cornish-Fisher expansion (Abramowitz & Stegun
 //     26.7.5) about the normal quantile; v = 1, 2 use their closed forms.
+//     The Beta start value is the normal approximation with its skewness
+//     term; Beta(1, b) and Beta(a, 1) use their closed forms.
 // lgamma, log1p, exp, normcdfinv are CUDA's own functions.
 #pragma once
 
@@ -52,24 +54,29 @@ NZ_HD inline double incbeta_cf(double a, double b, double x) {
     return h;
 }
 
-// I_x(a, b) with y = 1 - x supplied separately (no cancellation near 1).
-NZ_HD inline double incbeta(double a, double b, double x, double y) {
+// I_x(a, b) with y = 1 - x supplied separately (no cancellation near 1);
+// lbeta = ln B(a, b) = lgamma(a) + lgamma(b) - lgamma(a + b).
+NZ_HD inline double incbeta_lb(double a, double b, double x, double y, double lbeta) {
     if (x <= 0.0) return 0.0;
     if (y <= 0.0) return 1.0;
-    const double lbt = lgamma(a + b) - lgamma(a) - lgamma(b) + a * log(x) + b * log(y);
-    const double bt = exp(lbt);
+    const double bt = exp(a * log(x) + b * log(y) - lbeta);
     if (x < (a + 1.0) / (a + b + 2.0)) return bt * incbeta_cf(a, b, x) / a;
     return 1.0 - bt * incbeta_cf(b, a, y) / b;
 }
 
 // Upper tail 1 - I_x(a, b) with the same arguments, accurate when small.
-NZ_HD inline double incbeta_upper(double a, double b, double x, double y) {
+NZ_HD inline double incbeta_upper_lb(double a, double b, double x, double y, double lbeta) {
     if (x <= 0.0) return 1.0;
     if (y <= 0.0) return 0.0;
-    const double lbt = lgamma(a + b) - lgamma(a) - lgamma(b) + a * log(x) + b * log(y);
-    const double bt = exp(lbt);
+    const double bt = exp(a * log(x) + b * log(y) - lbeta);
     if (x < (a + 1.0) / (a + b + 2.0)) return 1.0 - bt * incbeta_cf(a, b, x) / a;
     return bt * incbeta_cf(b, a, y) / b;
+}
+
+NZ_HD inline double log_beta(double a, double b) { return lgamma(a) + lgamma(b) - lgamma(a + b); }
+
+NZ_HD inline double incbeta(double a, double b, double x, double y) {
+    return incbeta_lb(a, b, x, y, log_beta(a, b));
 }
 
 // Probability that a Student-t variable with v dof exceeds t >= 0.
@@ -145,24 +152,37 @@ NZ_HD inline double beta_quantile(double q, double a, double b) {
     if (!(a > 0.0) || !(b > 0.0) || !(q >= 0.0 && q <= 1.0)) return NAN;
     if (q == 0.0) return 0.0;
     if (q == 1.0) return 1.0;
-    const double lbeta = lgamma(a) + lgamma(b) - lgamma(a + b);
-    // normal-approximation start, clamped into (0, 1)
-    const double mu = a / (a + b);
-    const double sd = sqrt(a * b / ((a + b) * (a + b) * (a + b + 1.0)));
-    double x = mu + sd * nz_normal_quantile(q);
+    // the one-parameter families in closed form -- I_x(1, b) = 1 - (1 - x)^b
+    // and I_x(a, 1) = x^a -- which are the Bayesian spanning bounds of every
+    // n where no run or every run spans (most n of an ensemble)
+    if (a == 1.0) return -expm1(log1p(-q) / b);
+    if (b == 1.0) return exp(log(q) / a);
+    const double lbeta = log_beta(a, b);
+    // start: the normal approximation with its first skewness correction
+    // (Cornish-Fisher, Abramowitz & Stegun 26.2.49 with the Beta's skewness),
+    // clamped into (0, 1)
+    const double s = a + b;
+    const double mu = a / s;
+    const double sd = sqrt(a * b / (s * s * (s + 1.0)));
+    const double skew = 2.0 * (b - a) * sqrt(s + 1.0) / ((s + 2.0) * sqrt(a * b));
+    const double z = nz_normal_quantile(q);
+    double x = mu + sd * (z + skew * (z * z - 1.0) / 6.0);
     double lo = 0.0, hi = 1.0;
     if (!(x > 0.0 && x < 1.0)) x = mu;
     for (int it = 0; it < 200; ++it) {
         const double y = 1.0 - x;
         // work on whichever tail is smaller for accuracy
         double g;
-        if (q < 0.5) g = incbeta(a, b, x, y) - q;
-        else g = (1.0 - q) - incbeta_upper(a, b, x, y);  // I - q written via the upper tail
+        if (q < 0.5) g = incbeta_lb(a, b, x, y, lbeta) - q;
+        else g = (1.0 - q) - incbeta_upper_lb(a, b, x, y, lbeta);  // I - q written via the upper tail
         if (g < 0.0) lo = x; else hi = x;
         const double ldens = (a - 1.0) * log(x) + (b - 1.0) * log1p(-x) - lbeta;
         double xn = x - g / exp(ldens);
-        if (!(xn > lo && xn < hi) || !isfinite(xn)) xn = 0.5 * (lo + hi);
-        if (fabs(xn - x) <= 1e-15 * fmax(x, 1e-300) || hi - lo <= 1e-16 * hi) { x = xn; break; }
+        const bool newton = xn > lo && xn < hi && isfinite(xn);
+        if (!newton) xn = 0.5 * (lo + hi);
+        // a Newton step of relative size d leaves an error of order d^2:
+        // below 1e-10 the new iterate is converged to double precision
+        if ((newton && fabs(xn - x) <= 1e-10 * fmax(x, 1e-300)) || hi - lo <= 1e-16 * hi) { x = xn; break; }
         x = xn;
     }
     return x;

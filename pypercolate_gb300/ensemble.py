@@ -249,19 +249,21 @@ class Ensemble:
             raise ValueError('ensemble was created with micro=False')
         torch = nat.torch_cuda()
         out = torch.empty((self.M + 1) * 21, dtype=torch.float64, device='cuda')
+        # normalised, field-major (2 = NZ_MICRO_FIELD_MAJOR): each value's rows contiguous
         st = nat.lib_handle().nz_microcanonical_finalize(
-            self._micro_struct(), self.N, self.M, int(self.spanning), float(alpha), 1,
+            self._micro_struct(), self.N, self.M, int(self.spanning), float(alpha), 1 | 2,
             nat.ptr(out), nat.stream_handle())
         nat.check(st, 'nz_microcanonical_finalize')
-        o = out.cpu().numpy().reshape(self.M + 1, 21)
+        o = out.cpu().numpy().reshape(21, self.M + 1)
+        pair = lambda j: np.stack([o[j], o[j + 1]], axis=1)  # noqa: E731
         ret = {'N': self.N, 'M': self.M}
         if self.spanning:
-            ret['spanning_cluster'] = o[:, 0].copy()
-            ret['spanning_cluster_ci'] = o[:, 1:3].copy()
-        ret['max_cluster_size'] = o[:, 3].copy()
-        ret['max_cluster_size_ci'] = o[:, 4:6].copy()
-        ret['moments'] = np.stack([o[:, 6 + 3 * k] for k in range(5)])
-        ret['moments_ci'] = np.stack([o[:, 7 + 3 * k:9 + 3 * k] for k in range(5)])
+            ret['spanning_cluster'] = o[0].copy()
+            ret['spanning_cluster_ci'] = pair(1)
+        ret['max_cluster_size'] = o[3].copy()
+        ret['max_cluster_size_ci'] = pair(4)
+        ret['moments'] = o[6:21:3].copy()
+        ret['moments_ci'] = np.stack([pair(7 + 3 * k) for k in range(5)])
         return ret
 
     def micro_sums(self):

@@ -198,3 +198,64 @@ def test_precision_codes():
     codes (0 FP64, 1 FP32 SIMT, 2 3xTF32 tensor cores)."""
     from pypercolate_gb300.ensemble import PRECISIONS
     assert PRECISIONS == ('fp64', 'fp32', 'tf32x3')
+
+
+def test_mix_workspace_by_reduction(lib):
+    """The two reductions of nz_mix need different scratch: per-run
+    checkpoint records (36 B per run and checkpoint) or per-lattice sums
+    (27 words per lattice and checkpoint); an unknown reduction is refused."""
+    from pypercolate_gb300 import _native as nat
+    L = nat.lib_handle()
+    spec = nat.NzMixSpec()
+    spec.grid_min, spec.grid_max, spec.chain_min, spec.chain_max = 8, 64, 100, 2000
+    spec.chain_share, spec.checkpoints = 2 ** 31, 64
+    runs, threads = 50000, 4096
+    classes = (64 - 8 + 1) + (2000 - 100 + 1)
+    spec.reduction = 0
+    rec = L.nz_mix_workspace_bytes(ctypes.byref(spec), runs, threads)
+    spec.reduction = 1
+    fused = L.nz_mix_workspace_bytes(ctypes.byref(spec), runs, threads)
+    assert rec - fused == pytest.approx(runs * 64 * 36 - classes * 64 * 27 * 8, abs=4096)
+    spec.reduction = 2
+    assert L.nz_mix_workspace_bytes(ctypes.byref(spec), runs, threads) == 0
+
+
+def test_beta_quantile_host_restatement_matches_scipy():
+    """The Beta quantiles of the microcanonical spanning bounds
+    (csrc/nz_math.cuh, host-compiled here): closed forms for Beta(1, b) and
+    Beta(a, 1), Newton from the skewness-corrected start elsewhere -- against
+    scipy.stats.beta.ppf over the run counts and k an ensemble produces."""
+    import shutil
+    import subprocess
+    import tempfile
+    st = pytest.importorskip('scipy.stats')
+    cxx = shutil.which('g++')
+    if cxx is None:
+        pytest.skip('no host C++ compiler')
+    src = ('#include <cmath>\n#define __host__\n#define __device__\nusing std::isfinite;\n'
+           '#include "%s"\n'
+           'extern "C" void bq(const double *q, const double *a, const double *b, double *o, int n)'
+           ' { for (int i = 0; i < n; ++i) o[i] = nz::beta_quantile(q[i], a[i], b[i]); }\n'
+           % os.path.join(REPO, 'pypercolate_gb300', 'csrc', 'nz_math.cuh'))
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, 'bq.cpp'), 'w') as f:
+            f.write(src)
+        so = os.path.join(d, 'bq.so')
+        subprocess.run([cxx, '-O2', '-std=c++17', '-shared', '-fPIC', os.path.join(d, 'bq.cpp'), '-o', so],
+                       check=True)
+        fn = ctypes.CDLL(so).bq
+        rng = np.random.default_rng(5)
+        q, a, b = [], [], []
+        for R in (1, 2, 60, 1000, 100000):
+            ks = np.unique(np.concatenate([np.arange(0, min(R, 20) + 1), R - np.arange(0, min(R, 20) + 1),
+                                           rng.integers(0, R + 1, 400)]))
+            for qq in (0.025, 0.975, 0.15865, 0.84135):
+                q += [qq] * len(ks)
+                a += list(ks + 1.0)
+                b += list(R - ks + 1.0)
+        q, a, b = (np.array(v, dtype=np.float64) for v in (q, a, b))
+        out = np.empty_like(q)
+        P = ctypes.POINTER(ctypes.c_double)
+        fn(q.ctypes.data_as(P), a.ctypes.data_as(P), b.ctypes.data_as(P), out.ctypes.data_as(P),
+           ctypes.c_int(len(q)))
+    np.testing.assert_allclose(out, st.beta.ppf(q, a, b), rtol=1e-9)

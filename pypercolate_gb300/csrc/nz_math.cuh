@@ -5,7 +5,8 @@
 // (percolate/percolate.py:564-566).  These are computed here on the device
 // from the mathematics:
 //   * the regularized incomplete beta function I_x(a, b) by its continued
-//     fraction (DLMF 8.17.22), evaluated with the modified Lentz method, and
+//     fraction (DLMF 8.17.22), evaluated by the forward recurrence of its
+//     convergents (division-free after an equivalence transformation), and
 //     the symmetry I_x(a, b) = 1 - I_{1-x}(b, a) outside its fast region;
 //   * Student-t CDF F(t; v) = 1 - I_{v/(v+t^2)}(v/2, 1/2) / 2 for t >= 0;
 //   * quantiles by Newton's method on the CDF inside a maintained bracket,
@@ -28,30 +29,39 @@ namespace nz {
 #define NZ_HD __host__ __device__
 #endif
 
-// Continued fraction of I_x(a, b) (without the prefactor), x < (a+1)/(a+b+2).
+// Continued fraction of I_x(a, b) (without the prefactor), x < (a+1)/(a+b+2):
+//   f = 1 / (1 + d_1 / (1 + d_2 / (1 + ...))),  d_j = p_j / q_j,
+//   d_1 = -(a + b) x / (a + 1),
+//   d_2m = m (b - m) x / ((a + 2m - 1)(a + 2m)),
+//   d_2m+1 = -(a + m)(a + b + m) x / ((a + 2m)(a + 2m + 1)).
+// Evaluated by the forward recurrence of its convergents A_j / B_j after the
+// equivalence transformation that clears the q_j (partial numerators
+// q_{j-1} p_j, partial denominators q_j), so that no term needs a division
+// -- FP64 division is a long dependent sequence on this chip -- with A and B
+// rescaled by 1 / B every 8 terms (keeping them in range and A / B = A),
+// until two rescaled values agree to 1e-15.
 NZ_HD inline double incbeta_cf(double a, double b, double x) {
-    const double tiny = 1e-300, eps = 1e-16;
-    double c = 1.0;
-    double d = 1.0 - (a + b) * x / (a + 1.0);
-    if (fabs(d) < tiny) d = tiny;
-    d = 1.0 / d;
-    double h = d;
-    for (int m = 1; m <= 2000; ++m) {
-        const double m2 = 2.0 * m;
-        double aa = m * (b - m) * x / ((a + m2 - 1.0) * (a + m2));
-        d = 1.0 + aa * d; if (fabs(d) < tiny) d = tiny;
-        c = 1.0 + aa / c; if (fabs(c) < tiny) c = tiny;
-        d = 1.0 / d;
-        h *= d * c;
-        aa = -(a + m) * (a + b + m) * x / ((a + m2) * (a + m2 + 1.0));
-        d = 1.0 + aa * d; if (fabs(d) < tiny) d = tiny;
-        c = 1.0 + aa / c; if (fabs(c) < tiny) c = tiny;
-        d = 1.0 / d;
-        const double del = d * c;
-        h *= del;
-        if (fabs(del - 1.0) < eps) break;
+    double Ap = 0.0, Ac = 1.0, Bp = 1.0, Bc = 1.0, ql = 1.0;
+    auto term = [&](double p, double q) {
+        const double An = q * Ac + ql * p * Ap, Bn = q * Bc + ql * p * Bp;
+        Ap = Ac; Ac = An; Bp = Bc; Bc = Bn; ql = q;
+    };
+    term(-(a + b) * x, a + 1.0);
+    double f = 1.0;
+    for (int m = 1; m <= 2000; m += 4) {
+        for (int i = 0; i < 4; ++i) {
+            const double mm = m + i, m2 = 2.0 * mm;
+            term(mm * (b - mm) * x, (a + m2 - 1.0) * (a + m2));
+            term(-(a + mm) * (a + b + mm) * x, (a + m2) * (a + m2 + 1.0));
+        }
+        if (!(Bc != 0.0) || !isfinite(Bc)) break;  // (not in the convergent region)
+        const double r = 1.0 / Bc;
+        Ap *= r; Ac *= r; Bp *= r; Bc = 1.0;
+        const bool done = fabs(Ac - f) <= 1e-15 * fabs(Ac);
+        f = Ac;
+        if (done) break;
     }
-    return h;
+    return f;
 }
 
 // I_x(a, b) with y = 1 - x supplied separately (no cancellation near 1);

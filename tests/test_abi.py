@@ -193,6 +193,30 @@ def test_surrogate_features():
     assert c[0, 3] == 1 and abs(c[0, 4] - np.arcsinh(-3.0)) < 1e-6
 
 
+def test_surrogate_target_transforms():
+    """The units the surrogate learns in: logit spanning probability (clipped
+    to [1e-6, 1 - 1e-6]), log strength, log susceptibility as is; `curves`
+    inverts them, and `train_se` carries the standard errors over to first
+    order (at most one logit unit where pi is within its error of 0 or 1)."""
+    from pypercolate_gb300 import surrogate as S
+    y = np.array([[0.0, 1e-3, 1.0], [0.5, 0.2, 2.0], [1.0, 0.9, -3.0], [0.25, 1e-13, 0.5]])
+    se = np.array([[1e-4, 1e-6, 1e-3], [5e-3, 1e-3, 1e-3], [1e-4, 1e-4, 1e-2], [1e-2, 1e-6, 1e-3]])
+    t = S.train_targets(y)
+    np.testing.assert_allclose(t[:, 0], [np.log(1e-6 / (1 - 1e-6)), 0.0, np.log((1 - 1e-6) / 1e-6),
+                                         np.log(1 / 3)], rtol=1e-9)
+    np.testing.assert_allclose(t[:, 1], np.log([1e-3, 0.2, 0.9, S.STRENGTH_FLOOR]), rtol=1e-12)
+    np.testing.assert_array_equal(t[:, 2], y[:, 2])
+    back = S.curves(t)
+    np.testing.assert_allclose(back[1:3, :2], y[1:3, :2], rtol=1e-12)
+    np.testing.assert_allclose(back[[0, 3], 0], [1e-6, 0.25], rtol=1e-9)
+    s = S.train_se(y, se)
+    np.testing.assert_allclose(s[:, 0], [1.0, 0.02, 1.0, 1e-2 / 0.1875], rtol=1e-12)
+    np.testing.assert_allclose(s[:, 1], [1e-3, 5e-3, 1e-4 / 0.9, 1e-6 / S.STRENGTH_FLOOR], rtol=1e-12)
+    np.testing.assert_array_equal(s[:, 2], se[:, 2])
+    # large logits do not overflow on the way back
+    assert np.all(np.isfinite(S.curves(np.array([[800.0, 0.0, 0.0], [-800.0, 0.0, 0.0]]))))
+
+
 def test_precision_codes():
     """Ensemble precision names in the order of nz_ensemble's conv_precision
     codes (0 FP64, 1 FP32 SIMT, 2 3xTF32 tensor cores)."""

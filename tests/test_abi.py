@@ -207,8 +207,9 @@ def test_surrogate_target_transforms():
     np.testing.assert_allclose(t[:, 1], np.log([1e-3, 0.2, 0.9, S.STRENGTH_FLOOR]), rtol=1e-12)
     np.testing.assert_array_equal(t[:, 2], y[:, 2])
     back = S.curves(t)
-    np.testing.assert_allclose(back[1:3, :2], y[1:3, :2], rtol=1e-12)
-    np.testing.assert_allclose(back[[0, 3], 0], [1e-6, 0.25], rtol=1e-9)
+    np.testing.assert_allclose(back[[1, 3], 0], y[[1, 3], 0], rtol=1e-12)
+    np.testing.assert_allclose(back[[0, 2], 0], [1e-6, 1 - 1e-6], rtol=1e-9)  # clipped
+    np.testing.assert_allclose(back[:3, 1], y[:3, 1], rtol=1e-12)
     s = S.train_se(y, se)
     np.testing.assert_allclose(s[:, 0], [1.0, 0.02, 1.0, 1e-2 / 0.1875], rtol=1e-12)
     np.testing.assert_allclose(s[:, 1], [1e-3, 5e-3, 1e-4 / 0.9, 1e-6 / S.STRENGTH_FLOOR], rtol=1e-12)

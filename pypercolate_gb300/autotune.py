@@ -104,7 +104,7 @@ def tune_mix(n_runs, grid=(8, 512), chain=(1024, 65536), chain_share=0.5, checkp
 def default_window(M, n_runs):
     """Record-window rows nz_ensemble picks by itself: ~32 GiB of 36-byte
     records per window, 256 .. M + 1 rows."""
-    return int(max(256, min(M + 1, 32.0 * (1 << 30) / (n_runs * 36))))
+    return int(min(M + 1, max(256, 32.0 * (1 << 30) / (n_runs * 36))))
 
 
 def ensemble_candidates(M, n_runs):
@@ -114,7 +114,7 @@ def ensemble_candidates(M, n_runs):
             'reduce_slices': 64 if n_runs >= 65536 else 16, 'window': w}
     out = [dict(base)]
     for key, vals in (('uf_block', (64, 32)), ('m2_tile', (16,)), ('conv_tile', (16,)), ('taper', (1,)),
-                      ('window', (max(256, w // 2), min(M + 1, (3 * w) // 2))),
+                      ('window', (min(M + 1, max(256, w // 2)), min(M + 1, (3 * w) // 2))),
                       ('reduce_slices', (16 if base['reduce_slices'] != 16 else 64, 256))):
         for v in vals:
             c = dict(base)
@@ -122,6 +122,19 @@ def ensemble_candidates(M, n_runs):
             if c not in out:
                 out.append(c)
     return out
+
+
+def combined_candidate(table):
+    """From [(candidate, ms), ...] whose first row is the defaults and whose
+    other rows each change the defaults: the defaults with every change that
+    was faster than them, the fastest change applied last (so it wins where
+    two changes set the same shape)."""
+    base, base_ms = table[0]
+    combo = dict(base)
+    for cand, ms in sorted(table[1:], key=lambda t: -t[1]):  # the best change last
+        if ms < base_ms:
+            combo.update({k: v for k, v in cand.items() if v != base[k]})
+    return combo
 
 
 def _time_ensemble(kind, length, ps, n_runs, precision, micro, model, cand, key, reps, warm=False):
@@ -184,11 +197,7 @@ def tune_ensemble(kind, length, ps, n_runs, precision='fp32', micro=True, model=
     if candidates is None and len(table) > 1:
         # the candidates change one shape at a time: also time every change
         # that beat the defaults, together
-        base, base_ms = table[0]
-        combo = dict(base)
-        for cand, ms in sorted(table[1:], key=lambda t: -t[1]):  # the best change last
-            if ms < base_ms:
-                combo.update({k: v for k, v in cand.items() if v != base[k]})
+        combo = combined_candidate(table)
         if combo not in [c for c, _ in table]:
             table.append((combo, _time_ensemble(kind, length, ps, n_runs, precision, micro, model,
                                                 combo, key, reps)))

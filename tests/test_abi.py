@@ -284,3 +284,30 @@ def test_beta_quantile_host_restatement_matches_scipy():
         fn(q.ctypes.data_as(P), a.ctypes.data_as(P), b.ctypes.data_as(P), out.ctypes.data_as(P),
            ctypes.c_int(len(q)))
     np.testing.assert_allclose(out, st.beta.ppf(q, a, b), rtol=1e-9)
+
+
+def test_ensemble_tuner_candidates():
+    """The main path's autotuner: the library's defaults first, then one
+    launch-shape change at a time (no duplicates, windows within [256, M+1]),
+    and the combination of every change that beat the defaults."""
+    from pypercolate_gb300 import autotune as A
+    M, runs = 130560, 100000
+    w = A.default_window(M, runs)
+    assert w == int(32.0 * 2 ** 30 / (runs * 36))
+    assert A.default_window(100, runs) == 101 and A.default_window(10 ** 7, 10 ** 8) == 256
+    cands = A.ensemble_candidates(M, runs)
+    base = cands[0]
+    assert base == {'uf_block': 128, 'm2_tile': 8, 'conv_tile': 8, 'taper': 0, 'reduce_slices': 64,
+                    'window': w}
+    assert len(cands) == len({tuple(sorted(c.items())) for c in cands})
+    for c in cands[1:]:
+        assert sum(c[k] != base[k] for k in base) == 1
+        assert 256 <= c['window'] <= M + 1
+    table = [(base, 100.0), (dict(base, uf_block=64), 99.0), (dict(base, m2_tile=16), 101.0),
+             (dict(base, window=w // 2), 98.0), (dict(base, window=3 * w // 2), 99.5)]
+    combo = A.combined_candidate(table)
+    assert combo == dict(base, uf_block=64, window=w // 2)
+    assert A.combined_candidate([(base, 1.0), (dict(base, taper=1), 2.0)]) == base
+    # a lattice with fewer rows than the smallest window: every window is M + 1
+    small = A.ensemble_candidates(180, runs)
+    assert {c['window'] for c in small} == {181}
